@@ -1,0 +1,340 @@
+"""Benchmark of the D2Q9 collide-stream step on GB300.
+
+Workload (the configuration the headline metric is quoted on): lid-driven
+cavity, 1024 x 1024, MRT (the reference's rate set), lid u = 0.1 as a
+half-way moving wall, half-way bounce-back on the other walls, Re = 1000
+(nu = u L / Re with L = NY, src/main.cu:66), rho = 1 and u = 0 initially.
+
+  value     MLUPS of the fused step kernel, FP32 storage, inputs resident in
+            HBM; every timed step is preceded by a 256 MB write that flushes
+            L2 (the 1024^2 lattice, 38 MB per population set, would
+            otherwise stay in the 129 MB L2).
+  e2e       the same metric through the C-ABI with host buffers: fields
+            uploaded from pinned host memory, lbmx_step once per LBM step
+            with the FP64 mass/momentum sums read back every step (the
+            reference copies its moment averages back every step,
+            macroscopics.cuh:177), final density and velocity read back.
+  variants  FP16 / BF16 offset storage on the same workload, each with the
+            relative L2 velocity error against the FP64 oracle after 200
+            steps.
+  hbm_bound the same kernel on an 8192 x 8192 cavity (2.4 GB per population
+            set, far above L2) for the roofline fraction without a flush.
+  cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on the same
+            workload, 200 steps.
+
+`--impl reference` times the CPU implementation of the reference step (the
+oracle port; the reference itself has no CPU path) on this workload.
+Under torchrun each rank advances its own lattice replica (the path needs no
+collective on one lattice per GPU); value is the sum over ranks with the
+maximum per-rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "cuda-lbm_gb300"), os.path.join(REPO, "oracle"), os.path.join(REPO, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "MLUPS (D2Q9 lid-driven cavity 1024x1024 MRT, FP32 storage)"
+BYTES_PER_LU = {0: 72, 1: 36, 2: 36}
+STORAGE_NAME = {0: "f32", 1: "f16_offset", 2: "bf16_offset"}
+
+
+def cavity_case(n, storage=0):
+    import cases as C
+    nu = 0.1 * n / 1000.0
+    return C.cavity_moving_wall(n, n, op=C.MRT, nu=nu, u_lid=0.1)
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_steps(L, torch, stream, steps, warmup, flush):
+    """Per-step CUDA-event time (ms) of `steps` single LBM steps, each after an L2 flush."""
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            if flush is not None:
+                flush.zero_()
+            L.step(1, flags=0)
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for s, e in evs:
+            if flush is not None:
+                flush.zero_()
+            s.record(stream)
+            L.step(1, flags=0)
+            e.record(stream)
+        stream.synchronize()
+    return np.array([s.elapsed_time(e) for s, e in evs])
+
+
+def l2_error(u, uref):
+    return float(np.sqrt(((u - uref) ** 2).sum() / (uref ** 2).sum()))
+
+
+def run_cpu_oracle(n, steps, threads):
+    import cases as C
+    o = C.make_oracle(cavity_case(n))
+    o.step(1)
+    t0 = time.perf_counter()
+    o.step(steps - 1)
+    dt = time.perf_counter() - t0
+    _, u, _ = o.moments()
+    return u, (n * n * (steps - 1)) / dt / 1e6, dt
+
+
+def bench_reference(args, rank, world):
+    """CPU implementation of the reference step (the oracle port), all host threads."""
+    if rank != 0:
+        return
+    import cases as C
+    cores = os.cpu_count() or 1
+    n = args.size
+    c = cavity_case(n)
+    o = C.make_oracle(c)
+    per_step = args.ref_lbm_steps
+    for _ in range(args.warmup):
+        o.step(per_step)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.step(per_step)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    mlups = n * n * per_step / t / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3 / per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "lid-driven cavity %dx%d MRT, lid 0.1, Re 1000" % (n, n), "nodes": n * n,
+                   "lbm_steps_per_bench_step": per_step},
+        "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": "%d bench steps x %d LBM steps of the %dx%d cavity" % (args.steps, per_step, n, n)},
+        "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="lbmx", choices=["lbmx", "reference"])
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--hbm-size", type=int, default=8192)
+    ap.add_argument("--err-steps", type=int, default=200)
+    ap.add_argument("--ref-lbm-steps", type=int, default=5)
+    ap.add_argument("--quick", action="store_true", help="main number only (profiling runs)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        bench_reference(args, rank, world)
+        return
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import cases as C
+    import lbmx
+
+    stream = torch.cuda.Stream()
+    n = args.size
+    nodes = n * n
+    peaks, peak_kind = measured_peaks()
+    hbm = float(peaks["hbm_gbs"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def lattice(storage, size=n):
+        c = cavity_case(size)
+        L = lbmx.Lattice(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], storage=storage,
+                         wall_u=c["wall_u"], device=local, stream=stream.cuda_stream)
+        L.set_flags(c["flags"])
+        L.init(np.ones((c["ny"], c["nx"]), np.float32), np.zeros((2, c["ny"], c["nx"]), np.float32))
+        return L
+
+    # ---- headline: FP32, L2 flushed before every timed step
+    L = lattice(0)
+    with ClockSampler(local) as clk:
+        t = time_steps(L, torch, stream, args.steps, args.warmup, flush)
+    ms = float(t.mean())
+    if dist is not None:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    mlups = world * nodes / (ms * 1e-3) / 1e6
+    achieved = BYTES_PER_LU[0] * nodes / (float(t.mean()) * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "lid-driven cavity %dx%d, D2Q9 MRT, lid 0.1 half-way moving wall, Re 1000" % (n, n),
+                   "nodes": nodes, "storage": "f32", "l2": "flushed: 256 MB write before every timed step",
+                   "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "algorithmic_bytes_per_lu": BYTES_PER_LU[0], "peak_kind": peak_kind + " burst (hbm_gbs)"},
+        "gpu_launches": int(args.steps),
+        "clocks": clk.summary(),
+    }
+    prof = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            tr = json.load(fh)
+        if str(n) in tr:
+            line["roofline"]["traffic"] = tr[str(n)]
+
+    if rank == 0 and not args.quick:
+        # ---- e2e through the C-ABI with pinned host buffers
+        c = cavity_case(n)
+        h_rho = torch.ones((n, n), dtype=torch.float32).pin_memory()
+        h_u = torch.zeros((2, n, n), dtype=torch.float32).pin_memory()
+        h_flags = torch.from_numpy(c["flags"]).pin_memory()
+        out_rho = torch.empty((n, n), dtype=torch.float32).pin_memory()
+        out_u = torch.empty((2, n, n), dtype=torch.float32).pin_memory()
+        Le = lbmx.Lattice(n, n, op=c["op"], omega=c["omega"], S=c["S"], wall_u=c["wall_u"], device=local,
+                          stream=stream.cuda_stream)
+        import ctypes
+        sums = (ctypes.c_double * 3)()
+        K = args.steps
+        for rep in range(2):  # first pass warms up
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Le.set_flags(h_flags)
+            Le.init(h_rho, h_u)
+            for _ in range(K):
+                Le.lib.lbmx_step(Le.h, 1)
+                Le._check(Le.lib.lbmx_moments(Le.h, None, None, sums))
+            Le._check(Le.lib.lbmx_moments(Le.h, out_rho.data_ptr(), out_u.data_ptr(), sums))
+            e2e_t = time.perf_counter() - t0
+        line["e2e"] = {"value": round(nodes * K / e2e_t / 1e6, 1), "unit": "MLUPS",
+                       "h2d_bytes_per_step": int(round(13 * nodes / K)),
+                       "d2h_bytes_per_step": int(round(24 + 12 * nodes / K)),
+                       "lbm_steps": K, "seconds": round(e2e_t, 4)}
+        del Le
+
+        # ---- FP64 oracle: L2 error reference and CPU baseline
+        cores = os.cpu_count() or 1
+        u64, cpu_mlups, cpu_dt = run_cpu_oracle(n, args.err_steps, cores)
+        line["cpu_baseline"] = {"value": round(cpu_mlups, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
+                                "sample": "%d steps of the %dx%d cavity, FP64 oracle, OpenMP" % (args.err_steps, n, n)}
+
+        # ---- storage variants with the L2 error against FP64
+        variants = {}
+        for storage in (0, 1, 2):
+            Lv = lattice(storage)
+            tv = time_steps(Lv, torch, stream, args.steps, args.warmup, flush)
+            Lw = lattice(storage)
+            Lw.step(args.err_steps)
+            _, uv, _ = Lw.moments()
+            mv = nodes / (float(tv.mean()) * 1e-3) / 1e6
+            av = BYTES_PER_LU[storage] * nodes / (float(tv.mean()) * 1e-3) / 1e9
+            variants[STORAGE_NAME[storage]] = {
+                "MLUPS": round(mv, 1), "ms_per_step": round(float(tv.mean()), 5),
+                "achieved_GBs": round(av, 1), "frac": round(av / hbm, 4),
+                "l2_u_err_vs_fp64": l2_error(uv, u64), "err_steps": args.err_steps}
+            del Lv, Lw
+        variants["f16_speedup_vs_f32"] = round(variants["f16_offset"]["MLUPS"] / variants["f32"]["MLUPS"], 3)
+        line["variants"] = variants
+
+        # ---- HBM-bound size, no flush needed
+        hn = args.hbm_size
+        Lh = lattice(0, hn)
+        th = time_steps(Lh, torch, stream, max(10, args.steps // 5), args.warmup, None)
+        del Lh
+        Lh16 = lattice(1, hn)
+        th16 = time_steps(Lh16, torch, stream, max(10, args.steps // 5), args.warmup, None)
+        del Lh16
+        a32 = 72 * hn * hn / (float(th.mean()) * 1e-3) / 1e9
+        a16 = 36 * hn * hn / (float(th16.mean()) * 1e-3) / 1e9
+        line["hbm_bound"] = {
+            "workload": "lid-driven cavity %dx%d MRT" % (hn, hn),
+            "f32": {"MLUPS": round(hn * hn / (float(th.mean()) * 1e-3) / 1e6, 1), "achieved_GBs": round(a32, 1),
+                    "frac": round(a32 / hbm, 4)},
+            "f16_offset": {"MLUPS": round(hn * hn / (float(th16.mean()) * 1e-3) / 1e6, 1),
+                           "achieved_GBs": round(a16, 1), "frac": round(a16 / hbm, 4)},
+        }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,589 @@
+// lbmx_api.cu -- the C-ABI of liblbmx.so: handle lifetime, uploads, the
+// per-step launch sequence, readback and error reporting.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "lbmx.h"
+#include "lbmx_internal.h"
+
+namespace lbmx {
+size_t ibm_smem_bytes(int npatch, int nm);
+}
+
+using namespace lbmx;
+
+struct lbmx_handle {
+    lbmx_params p;
+    Geometry g;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void* f = nullptr;
+    int nplanes = 9;
+    uint8_t* flags = nullptr;      // device, pitched; null while every node is fluid
+    bool has_aux_bc = false;
+    float* edge = nullptr;         // [2][perimeter][9]
+    float* aux = nullptr;          // [perimeter][9]
+    float* force = nullptr;        // [2][plane] optional per-node body force
+    float* ibm_force = nullptr;    // [2][plane]
+    float* rho_out = nullptr;      // [plane]
+    float* u_out = nullptr;        // [2][plane]
+    float* staging = nullptr;      // dense [3][n] upload / readback staging
+    float* pop_out = nullptr;      // dense [9][n] readback staging
+    double* partials = nullptr;    // [blocks][6]
+    unsigned int* counter = nullptr;
+    double* sums = nullptr;        // [6]
+    float* avg = nullptr;          // [3]
+    unsigned int* error_word = nullptr;
+    long long blocks = 0;
+    long long t = 0;
+    bool initialized = false;
+    bool have_avg = false;
+    // immersed boundary
+    int nm = 0, npatch = 0, stencil = 0;
+    int* patch_nodes = nullptr;
+    int* sten_idx = nullptr;
+    float* sten_w = nullptr;
+    float* patch_rho = nullptr;
+    float* patch_u = nullptr;
+    float* marker_u = nullptr;
+    float* marker_rho = nullptr;
+    float* marker_force = nullptr;
+    char err[512] = {0};
+};
+
+static char g_create_err[512];
+
+static lbmx_status fail(lbmx_handle* h, lbmx_status code, const char* fmt, ...) {
+    char* dst = h ? h->err : g_create_err;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(dst, 512, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define LBMX_CUDA(h, call)                                                                          \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail((h), e_ == cudaErrorMemoryAllocation ? LBMX_ERR_OUT_OF_MEMORY : LBMX_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);        \
+    } while (0)
+
+static size_t elem_size(int storage) { return storage == LBMX_STORAGE_F32 ? 4 : 2; }
+
+template <typename Fn>
+static cudaError_t dispatch(int storage, Fn fn) {
+    switch (storage) {
+    case LBMX_STORAGE_F16_OFFSET: return fn(__half());
+    case LBMX_STORAGE_BF16_OFFSET: return fn(__nv_bfloat16());
+    default: return fn(float());
+    }
+}
+
+static StepArgs base_args(const lbmx_handle* h) {
+    StepArgs a;
+    memset(&a, 0, sizeof(a));
+    a.g = h->g;
+    a.f = h->f;
+    a.flags = h->flags;
+    a.edge = h->edge;
+    a.aux = h->aux;
+    a.force = h->force;
+    a.ibm_force = h->nm > 0 ? h->ibm_force : nullptr;
+    a.avg = h->avg;
+    a.quirks = h->p.quirks;
+    a.omega = h->p.omega;
+    for (int i = 0; i < 9; i++) a.S[i] = h->p.S[i];
+    a.u_bc = h->p.u_bc;
+    a.wall_ux = h->p.wall_ux;
+    a.wall_uy = h->p.wall_uy;
+    a.rho_out_bc = h->p.rho_out;
+    a.body_fx = h->p.body_fx;
+    a.body_fy = h->p.body_fy;
+    return a;
+}
+
+// parity and rest-population plane of step index s (1-based)
+static void set_step(const lbmx_handle* h, StepArgs& a, long long s) {
+    a.parity = (int)(s & 1);
+    a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? (a.parity ? 9 : 0) : 0;
+}
+
+static void free_ibm(lbmx_handle* h) {
+    cudaFree(h->patch_nodes); cudaFree(h->sten_idx); cudaFree(h->sten_w);
+    cudaFree(h->patch_rho); cudaFree(h->patch_u); cudaFree(h->marker_u);
+    cudaFree(h->marker_rho); cudaFree(h->marker_force); cudaFree(h->ibm_force);
+    h->patch_nodes = nullptr; h->sten_idx = nullptr; h->sten_w = nullptr;
+    h->patch_rho = h->patch_u = h->marker_u = h->marker_rho = h->marker_force = h->ibm_force = nullptr;
+    h->nm = h->npatch = 0;
+}
+
+extern "C" {
+
+int32_t lbmx_version(void) { return LBMX_VERSION; }
+
+void lbmx_params_default(lbmx_params* p) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->op = LBMX_BGK;
+    p->storage = LBMX_STORAGE_F32;
+    p->ibm_iters = 3;
+    p->omega = 1.0f;
+    for (int i = 0; i < 9; i++) p->S[i] = 1.0f;
+    p->rho_out = 1.0f;
+    p->ibm_ds = 1.0f;
+}
+
+void lbmx_destroy(lbmx_handle* h) {
+    if (!h) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(h->p.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_ibm(h);
+    cudaFree(h->f); cudaFree(h->flags); cudaFree(h->edge); cudaFree(h->aux);
+    cudaFree(h->force); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
+    cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums);
+    cudaFree(h->avg); cudaFree(h->error_word);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    cudaSetDevice(cur);
+    delete h;
+}
+
+lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
+    if (!out) return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: out is NULL");
+    *out = nullptr;
+    if (!p) return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: params is NULL");
+    if (p->nx < 3 || p->ny < 3)
+        return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: nx, ny must be >= 3 (got %d x %d)", p->nx, p->ny);
+    if ((long long)p->nx * p->ny > (1LL << 31) - 1)
+        return fail(nullptr, LBMX_ERR_TOO_LARGE, "lbmx_create: %d x %d nodes exceeds 2^31-1", p->nx, p->ny);
+    if (p->op < LBMX_BGK || p->op > LBMX_CM_OPT)
+        return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: unknown operator %d", p->op);
+    if (p->storage < LBMX_STORAGE_F32 || p->storage > LBMX_STORAGE_BF16_OFFSET)
+        return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: unknown storage %d", p->storage);
+    if (cudaSetDevice(p->device) != cudaSuccess)
+        return fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: cannot select device %d", p->device);
+    lbmx_handle* h = new lbmx_handle();
+    h->p = *p;
+    if (h->p.ibm_iters <= 0) h->p.ibm_iters = 3;
+    if (h->p.ibm_ds == 0.0f) h->p.ibm_ds = 1.0f;
+    Geometry& g = h->g;
+    g.nx = p->nx;
+    g.ny = p->ny;
+    g.pitch = (p->nx + 63) / 64 * 64;
+    g.periodic_x = p->periodic_x ? 1 : 0;
+    g.periodic_y = p->periodic_y ? 1 : 0;
+    g.plane = (long long)g.ny * g.pitch;
+    g.perimeter = 2 * g.nx + 2 * (g.ny - 2);
+    h->nplanes = (p->quirks & LBMX_QUIRK_REST_LAG) ? 10 : 9;
+    const long long n = (long long)g.nx * g.ny;
+    h->blocks = (long long)((g.nx + kBlockX - 1) / kBlockX) * ((g.ny + kBlockY - 1) / kBlockY);
+#define ALLOC(ptr, bytes)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));                               \
+        if (e_ != cudaSuccess) {                                                            \
+            fail(nullptr, LBMX_ERR_OUT_OF_MEMORY, "lbmx_create: cudaMalloc(%zu): %s",       \
+                 (size_t)(bytes), cudaGetErrorString(e_));                                  \
+            lbmx_destroy(h);                                                                \
+            return LBMX_ERR_OUT_OF_MEMORY;                                                  \
+        }                                                                                   \
+    } while (0)
+    ALLOC(h->f, (size_t)h->nplanes * g.plane * elem_size(p->storage));
+    ALLOC(h->edge, (size_t)2 * g.perimeter * 9 * sizeof(float));
+    ALLOC(h->aux, (size_t)g.perimeter * 9 * sizeof(float));
+    ALLOC(h->rho_out, (size_t)g.plane * sizeof(float));
+    ALLOC(h->u_out, (size_t)2 * g.plane * sizeof(float));
+    ALLOC(h->staging, (size_t)3 * n * sizeof(float));
+    ALLOC(h->partials, (size_t)h->blocks * 6 * sizeof(double));
+    ALLOC(h->counter, sizeof(unsigned int));
+    ALLOC(h->sums, 6 * sizeof(double));
+    ALLOC(h->avg, 3 * sizeof(float));
+    ALLOC(h->error_word, sizeof(unsigned int));
+#undef ALLOC
+    if (p->stream) {
+        h->stream = (cudaStream_t)p->stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: cudaStreamCreate failed");
+            lbmx_destroy(h);
+            return LBMX_ERR_CUDA;
+        }
+        h->own_stream = true;
+    }
+    cudaMemsetAsync(h->counter, 0, sizeof(unsigned int), h->stream);
+    cudaMemsetAsync(h->sums, 0, 6 * sizeof(double), h->stream);
+    cudaMemsetAsync(h->avg, 0, 3 * sizeof(float), h->stream);
+    cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream);
+    cudaMemsetAsync(h->aux, 0, (size_t)g.perimeter * 9 * sizeof(float), h->stream);
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: initial clears failed");
+        lbmx_destroy(h);
+        return LBMX_ERR_CUDA;
+    }
+    *out = h;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_set_flags(lbmx_handle* h, const uint8_t* flags) {
+    if (!h || !flags) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_flags: NULL argument");
+    cudaSetDevice(h->p.device);
+    const Geometry& g = h->g;
+    const long long n = (long long)g.nx * g.ny;
+    std::vector<uint8_t> hf(n);
+    LBMX_CUDA(h, cudaMemcpy(hf.data(), flags, n, cudaMemcpyDefault));
+    bool any = false, aux = false;
+    for (int y = 0; y < g.ny; y++)
+        for (int x = 0; x < g.nx; x++) {
+            const uint8_t fl = hf[(long long)y * g.nx + x];
+            if (fl == 0) continue;
+            any = true;
+            const bool edge = x == 0 || y == 0 || x == g.nx - 1 || y == g.ny - 1;
+            if (fl == LBMX_ZOU_HE_TOP_LEFT_TOP_INFLOW || fl == LBMX_ZOU_HE_TOP_RIGHT_TOP_INFLOW)
+                return fail(h, LBMX_ERR_INVALID_FLAGS,
+                            "lbmx_set_flags: flag %d at (%d,%d) is not implemented by the reference (it asserts)", fl, x, y);
+            if (fl > LBMX_HALFWAY_BB)
+                return fail(h, LBMX_ERR_INVALID_FLAGS, "lbmx_set_flags: unknown flag %d at (%d,%d)", fl, x, y);
+            if (fl == LBMX_PRESSURE_OUTLET && (!edge || x == 0))
+                return fail(h, LBMX_ERR_INVALID_FLAGS,
+                            "lbmx_set_flags: PRESSURE_OUTLET at (%d,%d) must sit on the domain edge with x >= 1", x, y);
+            if ((fl == LBMX_ZG_OUTFLOW || fl == LBMX_REGULARIZED_BOUNCE_BACK_CORNER) && edge) aux = true;
+            if (fl == LBMX_PRESSURE_OUTLET) aux = true;
+        }
+    if (!any) {
+        cudaFree(h->flags);
+        h->flags = nullptr;
+        h->has_aux_bc = false;
+        return LBMX_OK;
+    }
+    if (!h->flags) {
+        cudaError_t e = cudaMalloc((void**)&h->flags, (size_t)g.plane);
+        if (e != cudaSuccess) return fail(h, LBMX_ERR_OUT_OF_MEMORY, "lbmx_set_flags: cudaMalloc failed");
+    }
+    LBMX_CUDA(h, cudaMemsetAsync(h->flags, 0, (size_t)g.plane, h->stream));
+    LBMX_CUDA(h, cudaMemcpy2DAsync(h->flags, g.pitch, hf.data(), g.nx, g.nx, g.ny, cudaMemcpyHostToDevice, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->has_aux_bc = aux;
+    return LBMX_OK;
+}
+
+static lbmx_status upload_force(lbmx_handle* h, const float* force) {
+    const Geometry& g = h->g;
+    const long long n = (long long)g.nx * g.ny;
+    if (!force) {
+        cudaFree(h->force);
+        h->force = nullptr;
+        return LBMX_OK;
+    }
+    std::vector<float> hf(2 * n);
+    LBMX_CUDA(h, cudaMemcpy(hf.data(), force, 2 * n * sizeof(float), cudaMemcpyDefault));
+    bool uniform = true;
+    for (long long i = 1; i < n && uniform; i++)
+        uniform = hf[i] == hf[0] && hf[n + i] == hf[n];
+    if (uniform) {
+        // the common case (every reference scenario): no per-node force reads
+        h->p.body_fx = hf[0];
+        h->p.body_fy = hf[n];
+        cudaFree(h->force);
+        h->force = nullptr;
+        return LBMX_OK;
+    }
+    if (!h->force) {
+        cudaError_t e = cudaMalloc((void**)&h->force, (size_t)2 * g.plane * sizeof(float));
+        if (e != cudaSuccess) return fail(h, LBMX_ERR_OUT_OF_MEMORY, "force field: cudaMalloc failed");
+    }
+    LBMX_CUDA(h, cudaMemsetAsync(h->force, 0, (size_t)2 * g.plane * sizeof(float), h->stream));
+    for (int c = 0; c < 2; c++)
+        LBMX_CUDA(h, cudaMemcpy2DAsync(h->force + c * g.plane, g.pitch * sizeof(float), hf.data() + c * n,
+                                       g.nx * sizeof(float), g.nx * sizeof(float), g.ny, cudaMemcpyHostToDevice,
+                                       h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_set_force_field(lbmx_handle* h, const float* force) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_force_field: NULL handle");
+    cudaSetDevice(h->p.device);
+    return upload_force(h, force);
+}
+
+lbmx_status lbmx_init_from_fields(lbmx_handle* h, const float* rho, const float* u, const float* force) {
+    if (!h || !rho || !u) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_init_from_fields: NULL argument");
+    cudaSetDevice(h->p.device);
+    const Geometry& g = h->g;
+    const long long n = (long long)g.nx * g.ny;
+    LBMX_CUDA(h, cudaMemcpyAsync(h->staging, rho, n * sizeof(float), cudaMemcpyDefault, h->stream));
+    LBMX_CUDA(h, cudaMemcpyAsync(h->staging + n, u, 2 * n * sizeof(float), cudaMemcpyDefault, h->stream));
+    if (force) {
+        lbmx_status st = upload_force(h, force);
+        if (st != LBMX_OK) return st;
+    }
+    StepArgs a = base_args(h);
+    a.rho_out = h->rho_out;
+    a.u_out = h->u_out;
+    a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? 9 : 0;
+    LBMX_CUDA(h, cudaMemsetAsync(h->rho_out, 0, (size_t)g.plane * sizeof(float), h->stream));
+    LBMX_CUDA(h, cudaMemsetAsync(h->u_out, 0, (size_t)2 * g.plane * sizeof(float), h->stream));
+    LBMX_CUDA(h, dispatch(h->p.storage, [&](auto tag) {
+                  return launch_init<decltype(tag)>(a, h->staging, h->staging + n, h->stream);
+              }));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->t = 0;
+    h->initialized = true;
+    h->have_avg = false;
+    return LBMX_OK;
+}
+
+// One step (index s = t+1); store: write moments and FP64 sums.
+static lbmx_status run_step(lbmx_handle* h, bool store, bool check) {
+    const long long s = h->t + 1;
+    StepArgs a = base_args(h);
+    set_step(h, a, s);
+    cudaStream_t st = h->stream;
+    const int storage = h->p.storage;
+    if (h->has_aux_bc)
+        LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_edge_prepass<decltype(tag)>(a, h->aux, st); }));
+    if (h->nm > 0) {
+        LBMX_CUDA(h, dispatch(storage, [&](auto tag) {
+                      return launch_ibm_gather<decltype(tag)>(a, h->patch_nodes, h->npatch, h->patch_rho, h->patch_u, st);
+                  }));
+        IbmArgs ia;
+        ia.nm = h->nm;
+        ia.npatch = h->npatch;
+        ia.iters = h->p.ibm_iters;
+        ia.stencil = h->stencil;
+        ia.sten_idx = h->sten_idx;
+        ia.sten_w = h->sten_w;
+        ia.patch_nodes = h->patch_nodes;
+        ia.patch_rho = h->patch_rho;
+        ia.patch_u = h->patch_u;
+        ia.marker_u = h->marker_u;
+        ia.marker_rho = h->marker_rho;
+        ia.marker_force = h->marker_force;
+        ia.ibm_force = h->ibm_force;
+        ia.plane = h->g.plane;
+        ia.clamp = (h->p.quirks & LBMX_QUIRK_IBM_CLAMP) ? 1 : 0;
+        ia.ds = h->p.ibm_ds;
+        LBMX_CUDA(h, launch_ibm_iterate(ia, st));
+    }
+    const bool opt = h->p.op == LBMX_CM_OPT;
+    const bool lagged = opt && (h->p.options & LBMX_OPTION_LAGGED_AVERAGES) && h->have_avg;
+    if (opt && !lagged) {
+        StepArgs b = a;
+        b.partials = h->partials;
+        b.counter = h->counter;
+        b.sums = nullptr;
+        b.avg_out = h->avg;
+        LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_opt_prepass<decltype(tag)>(b, st); }));
+        h->have_avg = true;
+    }
+    if (store) {
+        a.rho_out = h->rho_out;
+        a.u_out = h->u_out;
+    }
+    if (store || lagged) {
+        a.partials = h->partials;
+        a.counter = h->counter;
+        a.sums = store ? h->sums : nullptr;
+        // lagged CM_OPT: the averages of this step feed the next one
+        a.avg_out = lagged ? h->avg : nullptr;
+    }
+    if (check) a.error_word = h->error_word;
+    LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->p.op, st); }));
+    h->t = s;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step: NULL handle");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_step: call lbmx_init_from_fields first");
+    if (nsteps < 0) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step: nsteps < 0");
+    cudaSetDevice(h->p.device);
+    const bool check = (flags & LBMX_STEP_CHECK_FINITE) != 0;
+    if (check) LBMX_CUDA(h, cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream));
+    for (int i = 0; i < nsteps; i++) {
+        const bool last = i == nsteps - 1;
+        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check);
+        if (st != LBMX_OK) return st;
+    }
+    if (check) {
+        unsigned int w = 0;
+        LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
+        LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (w) return fail(h, LBMX_ERR_NONFINITE, "lbmx_step: non-finite density at step %lld", h->t);
+    }
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_step(lbmx_handle* h, int32_t nsteps) {
+    return lbmx_step_ex(h, nsteps, LBMX_STEP_STORE_MOMENTS);
+}
+
+lbmx_status lbmx_moments(lbmx_handle* h, float* rho, float* u, double* sums3) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_moments: NULL handle");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_moments: not initialized");
+    cudaSetDevice(h->p.device);
+    const Geometry& g = h->g;
+    const long long n = (long long)g.nx * g.ny;
+    if (rho)
+        LBMX_CUDA(h, cudaMemcpy2DAsync(rho, g.nx * sizeof(float), h->rho_out, g.pitch * sizeof(float),
+                                       g.nx * sizeof(float), g.ny, cudaMemcpyDefault, h->stream));
+    if (u)
+        for (int c = 0; c < 2; c++)
+            LBMX_CUDA(h, cudaMemcpy2DAsync(u + c * n, g.nx * sizeof(float), h->u_out + c * g.plane,
+                                           g.pitch * sizeof(float), g.nx * sizeof(float), g.ny, cudaMemcpyDefault,
+                                           h->stream));
+    if (sums3) {
+        double s[6];
+        LBMX_CUDA(h, cudaMemcpyAsync(s, h->sums, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+        LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+        sums3[0] = s[0];
+        sums3[1] = s[1];
+        sums3[2] = s[2];
+    }
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_get_populations(lbmx_handle* h, float* out) {
+    if (!h || !out) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_get_populations: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_get_populations: not initialized");
+    cudaSetDevice(h->p.device);
+    const long long n = (long long)h->g.nx * h->g.ny;
+    if (!h->pop_out) LBMX_CUDA(h, cudaMalloc((void**)&h->pop_out, (size_t)9 * n * sizeof(float)));
+    StepArgs a = base_args(h);
+    // parity and rest plane of the last step taken (init looks like a parity-0 step)
+    set_step(h, a, h->t);
+    if (h->t == 0) a.parity = 0;
+    LBMX_CUDA(h, dispatch(h->p.storage, [&](auto tag) {
+                  return launch_get_populations<decltype(tag)>(a, h->pop_out, h->stream);
+              }));
+    LBMX_CUDA(h, cudaMemcpyAsync(out, h->pop_out, (size_t)9 * n * sizeof(float), cudaMemcpyDefault, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_averages(lbmx_handle* h, float* avg3) {
+    if (!h || !avg3) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_averages: NULL argument");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaMemcpyAsync(avg3, h->avg, 3 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LBMX_OK;
+}
+
+// Peskin 4-point kernel (src/IBM/IBMUtils.cuh:24-33), evaluated in double on the host
+static double delta4(double r) {
+    const double a = std::fabs(r);
+    if (a < 1.0) return 0.125 * (3.0 - 2.0 * a + std::sqrt(1.0 + 4.0 * a - 4.0 * r * r));
+    if (a < 2.0) return 0.125 * (5.0 - 2.0 * a - std::sqrt(-7.0 + 12.0 * a - 4.0 * r * r));
+    return 0.0;
+}
+
+lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: NULL handle");
+    if (n < 0 || (n > 0 && !xy)) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: bad marker array");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    free_ibm(h);
+    if (n == 0) return LBMX_OK;
+    const Geometry& g = h->g;
+    std::vector<float> hxy(2 * (size_t)n);
+    LBMX_CUDA(h, cudaMemcpy(hxy.data(), xy, 2 * (size_t)n * sizeof(float), cudaMemcpyDefault));
+    const bool two = (h->p.quirks & LBMX_QUIRK_IBM_2X2) != 0;
+    const int S = two ? 2 : 4, lo = two ? 0 : -1, S2 = S * S;
+    std::vector<int> sidx((size_t)n * S2, -1);
+    std::vector<float> sw((size_t)n * S2, 0.f);
+    std::vector<int> nodes;
+    std::unordered_map<long long, int> map;
+    for (int k = 0; k < n; k++) {
+        const float px = hxy[2 * k], py = hxy[2 * k + 1];
+        if (!std::isfinite(px) || !std::isfinite(py))
+            return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: marker %d is not finite", k);
+        const float gx = std::floor(px), gy = std::floor(py);
+        // x offset outer, y offset inner, as the reference's stencil loops (IBM_impl.cu:19-20)
+        for (int i = 0; i < S; i++)
+            for (int j = 0; j < S; j++) {
+                const int xn = (int)(gx + (float)(lo + i)), yn = (int)(gy + (float)(lo + j));
+                if (xn < 0 || xn >= g.nx || yn < 0 || yn >= g.ny) continue;
+                const long long off = (long long)yn * g.pitch + xn;
+                auto it = map.find(off);
+                int idx;
+                if (it == map.end()) {
+                    idx = (int)nodes.size();
+                    map.emplace(off, idx);
+                    nodes.push_back((int)off);
+                } else {
+                    idx = it->second;
+                }
+                sidx[(size_t)k * S2 + i * S + j] = idx;
+                sw[(size_t)k * S2 + i * S + j] = (float)(delta4((double)px - xn) * delta4((double)py - yn));
+            }
+    }
+    const int np = (int)nodes.size();
+    if (lbmx::ibm_smem_bytes(np, n) > 200 * 1024)
+        return fail(h, LBMX_ERR_TOO_LARGE, "lbmx_ibm_set_markers: %d markers touch %d nodes; limit is 200 KB of patch state",
+                    n, np);
+    h->nm = n;
+    h->npatch = np;
+    h->stencil = S;
+    LBMX_CUDA(h, cudaMalloc((void**)&h->patch_nodes, np * sizeof(int)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->sten_idx, (size_t)n * S2 * sizeof(int)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->sten_w, (size_t)n * S2 * sizeof(float)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->patch_rho, np * sizeof(float)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->patch_u, 2 * (size_t)np * sizeof(float)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->marker_u, 2 * (size_t)n * sizeof(float)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->marker_rho, (size_t)n * sizeof(float)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->marker_force, 2 * (size_t)n * sizeof(float)));
+    LBMX_CUDA(h, cudaMalloc((void**)&h->ibm_force, 2 * (size_t)g.plane * sizeof(float)));
+    LBMX_CUDA(h, cudaMemcpy(h->patch_nodes, nodes.data(), np * sizeof(int), cudaMemcpyHostToDevice));
+    LBMX_CUDA(h, cudaMemcpy(h->sten_idx, sidx.data(), sidx.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LBMX_CUDA(h, cudaMemcpy(h->sten_w, sw.data(), sw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    LBMX_CUDA(h, cudaMemset(h->ibm_force, 0, 2 * (size_t)g.plane * sizeof(float)));
+    LBMX_CUDA(h, cudaMemset(h->marker_force, 0, 2 * (size_t)n * sizeof(float)));
+    LBMX_CUDA(h, cudaMemset(h->marker_u, 0, 2 * (size_t)n * sizeof(float)));
+    LBMX_CUDA(h, cudaMemset(h->marker_rho, 0, (size_t)n * sizeof(float)));
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_ibm_forces(lbmx_handle* h, float* force, double* drag_lift) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_forces: NULL handle");
+    cudaSetDevice(h->p.device);
+    std::vector<float> hf(2 * (size_t)h->nm);
+    if (h->nm > 0)
+        LBMX_CUDA(h, cudaMemcpyAsync(hf.data(), h->marker_force, hf.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                                     h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (force && h->nm > 0) memcpy(force, hf.data(), hf.size() * sizeof(float));
+    if (drag_lift) {
+        double dx = 0, dy = 0;
+        for (int k = 0; k < h->nm; k++) {
+            dx += hf[k];
+            dy += hf[h->nm + k];
+        }
+        drag_lift[0] = -dx;
+        drag_lift[1] = -dy;
+    }
+    return LBMX_OK;
+}
+
+int64_t lbmx_time(lbmx_handle* h) { return h ? h->t : -1; }
+
+lbmx_status lbmx_synchronize(lbmx_handle* h) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_synchronize: NULL handle");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LBMX_OK;
+}
+
+const char* lbmx_last_error(lbmx_handle* h) { return h ? h->err : g_create_err; }
+
+}  // extern "C"

@@ -1,0 +1,97 @@
+// lbmx_internal.h -- structures shared by the host launcher and the kernels.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace lbmx {
+
+// Geometry and storage of one lattice in HBM.
+//
+// Populations: plane-major SoA, plane q at f + q*plane, row pitch `pitch`
+// elements (a multiple of 32 so every row starts on a 128-byte line).  The
+// in-place AA streaming pattern keeps one buffer: after a step of parity 0
+// (and after init) slot OPP(q) of node x holds f*_q(x); after a step of
+// parity 1 slot q of node x+c_q holds f*_q(x).  Plane 9 exists only with
+// the rest-population quirk (f0 from two steps back, one plane per parity).
+//
+// Edge store: nodes on the domain perimeter keep, per parity, the
+// post-collision value of every population whose upstream node lies outside
+// a non-periodic domain; that value is what the reference's ping-pong
+// buffers hand back two steps later (src/core/streaming/streaming.cu:20-21).
+struct Geometry {
+    int nx, ny, pitch;
+    int periodic_x, periodic_y;
+    long long plane;   // elements per population plane (ny * pitch)
+    int perimeter;     // 2*nx + 2*(ny-2)
+};
+
+struct StepArgs {
+    Geometry g;
+    void* f;                 // population storage (float / __half / __nv_bfloat16)
+    const uint8_t* flags;    // [ny][pitch] boundary flags, nullptr if all fluid
+    float* edge;             // [2][perimeter][9]
+    const float* aux;        // [perimeter][9] neighbour data for ZG / pressure / corner
+    const float* force;      // [2][plane] per-node body force or nullptr
+    const float* ibm_force;  // [2][plane] IBM force (zero away from markers) or nullptr
+    const float* avg;        // CM_OPT grid averages {rho, |j|, |Pi|} (device)
+    float* rho_out;          // [plane] moments written when non-null
+    float* u_out;            // [2][plane]
+    double* partials;        // [blocks][6] FP64 block sums when non-null
+    unsigned int* counter;   // last-block-done counter for the sums
+    double* sums;            // [6] final sums
+    float* avg_out;          // averages produced by the last block (lagged CM_OPT / pre-pass)
+    unsigned int* error_word;// non-finite detection (nullptr: off)
+    uint32_t quirks;
+    int parity;              // step index & 1; 1 = neighbour-access phase
+    int rest_plane;          // plane that holds f0 this step (0 or 9)
+    float omega;
+    float S[9];
+    float u_bc, wall_ux, wall_uy, rho_out_bc;
+    float body_fx, body_fy;
+};
+
+// perimeter index of a node on the domain edge
+__host__ __device__ inline int edge_index(int x, int y, int nx, int ny) {
+    if (y == 0) return x;
+    if (y == ny - 1) return nx + x;
+    if (x == 0) return 2 * nx + (y - 1);
+    return 2 * nx + (ny - 2) + (y - 1);
+}
+
+// host launchers (one translation unit per storage type)
+template <typename T>
+cudaError_t launch_step(const StepArgs& a, int op, cudaStream_t s);
+template <typename T>
+cudaError_t launch_edge_prepass(const StepArgs& a, float* aux, cudaStream_t s);
+template <typename T>
+cudaError_t launch_opt_prepass(const StepArgs& a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_init(const StepArgs& a, const float* rho, const float* u, cudaStream_t s);
+template <typename T>
+cudaError_t launch_get_populations(const StepArgs& a, float* out, cudaStream_t s);
+template <typename T>
+cudaError_t launch_ibm_gather(const StepArgs& a, const int* patch_nodes, int npatch,
+                              float* patch_rho, float* patch_u, cudaStream_t s);
+
+// IBM multi-direct forcing on the marker patch (lbmx_ibm.cu)
+struct IbmArgs {
+    int nm, npatch, iters, stencil;     // stencil: 2 or 4 nodes per axis
+    const int* sten_idx;                // [nm][stencil^2] patch index or -1
+    const float* sten_w;                // [nm][stencil^2] kernel weight
+    const int* patch_nodes;             // [npatch] node offset (y*pitch + x)
+    const float* patch_rho;             // [npatch]
+    const float* patch_u;               // [2][npatch] uncorrected velocity
+    float* marker_u;                    // [2][nm] last interpolated velocity
+    float* marker_rho;                  // [nm]
+    float* marker_force;                // [2][nm] summed over iterations
+    float* ibm_force;                   // [2][plane] dense Eulerian force
+    long long plane;
+    int clamp;
+    float ds;
+};
+cudaError_t launch_ibm_iterate(const IbmArgs& a, cudaStream_t s);
+
+constexpr int kBlockX = 128;
+constexpr int kBlockY = 2;
+
+}  // namespace lbmx

@@ -1,0 +1,209 @@
+"""Python binding of liblbmx.so (the engine's C-ABI, include/lbmx.h).
+
+A thin ctypes layer: it loads the in-tree shared library (built by
+build.py) and mirrors the C entry points one to one.  Field arguments may be
+numpy arrays (host memory) or torch tensors (host or CUDA memory); the
+library copies with cudaMemcpyDefault either way.  There is no fallback:
+if the library cannot be loaded, importing fails loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbmx.so")
+
+# operators, storage, flags and quirks: the values of include/lbmx.h
+BGK, MRT, CM, CM_OPT = 0, 1, 2, 3
+F32, F16_OFFSET, BF16_OFFSET = 0, 1, 2
+FLUID, BOUNCE_BACK, ZOU_HE_TOP, ZOU_HE_LEFT = 0, 1, 2, 3
+CYLINDER, ZG_OUTFLOW, PRESSURE_OUTLET, REGULARIZED_INLET_TOP = 6, 7, 8, 9
+REGULARIZED_INLET_LEFT, REGULARIZED_BOUNCE_BACK, REGULARIZED_BOUNCE_BACK_CORNER = 10, 11, 12
+MOVING_WALL_BB, ZOU_HE_PRESSURE_RIGHT, ZOU_HE_PARABOLIC_LEFT, HALFWAY_BB = 32, 33, 34, 35
+QUIRK_REST_LAG, QUIRK_ZOUHE_LEFT, QUIRK_MRT_FORCE, QUIRK_IBM_2X2, QUIRK_IBM_CLAMP = 1, 2, 4, 8, 16
+QUIRKS_REFERENCE = 0x1F
+OPTION_LAGGED_AVERAGES = 1
+STEP_STORE_MOMENTS, STEP_CHECK_FINITE = 1, 2
+
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INVALID_FLAGS",
+          5: "NOT_INITIALIZED", 6: "UNSUPPORTED", 7: "NONFINITE", 8: "TOO_LARGE"}
+
+EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
+            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
+            "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
+            "lbmx_synchronize", "lbmx_last_error"]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+        ("periodic_x", ctypes.c_int32), ("periodic_y", ctypes.c_int32),
+        ("op", ctypes.c_int32), ("storage", ctypes.c_int32),
+        ("quirks", ctypes.c_uint32), ("options", ctypes.c_uint32),
+        ("ibm_iters", ctypes.c_int32), ("device", ctypes.c_int32),
+        ("omega", ctypes.c_float), ("S", ctypes.c_float * 9),
+        ("u_bc", ctypes.c_float), ("wall_ux", ctypes.c_float), ("wall_uy", ctypes.c_float),
+        ("rho_out", ctypes.c_float), ("ibm_ds", ctypes.c_float),
+        ("body_fx", ctypes.c_float), ("body_fy", ctypes.c_float),
+        ("stream", ctypes.c_void_p),
+    ]
+
+
+class LbmxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("lbmx error %d (%s): %s" % (code, STATUS.get(code, "?"), msg))
+        self.code = code
+
+
+def load_library(path=LIB_PATH):
+    """Load liblbmx.so and declare its signatures; raises OSError if absent."""
+    lib = ctypes.CDLL(path)
+    P, vp = ctypes.POINTER, ctypes.c_void_p
+    fp, dp = P(ctypes.c_float), P(ctypes.c_double)
+    lib.lbmx_version.restype = ctypes.c_int32
+    lib.lbmx_params_default.argtypes = [P(Params)]
+    lib.lbmx_create.argtypes = [P(Params), P(vp)]
+    lib.lbmx_destroy.argtypes = [vp]
+    lib.lbmx_set_flags.argtypes = [vp, vp]
+    lib.lbmx_init_from_fields.argtypes = [vp, vp, vp, vp]
+    lib.lbmx_set_force_field.argtypes = [vp, vp]
+    lib.lbmx_step.argtypes = [vp, ctypes.c_int32]
+    lib.lbmx_step_ex.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32]
+    lib.lbmx_moments.argtypes = [vp, vp, vp, dp]
+    lib.lbmx_get_populations.argtypes = [vp, vp]
+    lib.lbmx_averages.argtypes = [vp, fp]
+    lib.lbmx_ibm_set_markers.argtypes = [vp, vp, ctypes.c_int32]
+    lib.lbmx_ibm_forces.argtypes = [vp, fp, dp]
+    lib.lbmx_time.restype = ctypes.c_int64
+    lib.lbmx_time.argtypes = [vp]
+    lib.lbmx_synchronize.argtypes = [vp]
+    lib.lbmx_last_error.restype = ctypes.c_char_p
+    lib.lbmx_last_error.argtypes = [vp]
+    for name in ("lbmx_create", "lbmx_set_flags", "lbmx_init_from_fields", "lbmx_set_force_field",
+                 "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_get_populations", "lbmx_averages",
+                 "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_synchronize"):
+        getattr(lib, name).restype = ctypes.c_int32
+    return lib
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = load_library()
+    return _LIB
+
+
+def _ptr(a, dtype):
+    """Data pointer of a numpy array or torch tensor (host or CUDA), checked."""
+    if a is None:
+        return None, None
+    if hasattr(a, "data_ptr"):  # torch tensor
+        import torch
+        want = {np.float32: torch.float32, np.uint8: torch.uint8, np.float64: torch.float64}[dtype]
+        if a.dtype != want or not a.is_contiguous():
+            a = a.to(want).contiguous()
+        return a.data_ptr(), a
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a.ctypes.data, a
+
+
+class Lattice:
+    """One D2Q9 lattice on the GPU, driven through the C-ABI."""
+
+    def __init__(self, nx, ny, op=BGK, omega=1.0, S=None, periodic=(False, False), storage=F32,
+                 quirks=0, options=0, u_bc=0.0, wall_u=(0.0, 0.0), rho_out=1.0, ibm_iters=3, ibm_ds=1.0,
+                 body_force=(0.0, 0.0), device=0, stream=None):
+        self.lib = lib()
+        p = Params()
+        self.lib.lbmx_params_default(ctypes.byref(p))
+        p.nx, p.ny = nx, ny
+        p.periodic_x, p.periodic_y = int(bool(periodic[0])), int(bool(periodic[1]))
+        p.op, p.storage, p.quirks, p.options = op, storage, quirks, options
+        p.ibm_iters, p.device = ibm_iters, device
+        p.omega = omega
+        S = [omega] * 9 if S is None else S
+        for i in range(9):
+            p.S[i] = S[i]
+        p.u_bc, p.wall_ux, p.wall_uy, p.rho_out, p.ibm_ds = u_bc, wall_u[0], wall_u[1], rho_out, ibm_ds
+        p.body_fx, p.body_fy = body_force
+        p.stream = stream
+        self.params = p
+        h = ctypes.c_void_p()
+        rc = self.lib.lbmx_create(ctypes.byref(p), ctypes.byref(h))
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_last_error(None).decode())
+        self.h = h
+        self.nx, self.ny, self.n = nx, ny, nx * ny
+        self.nm = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbmx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_last_error(self.h).decode())
+
+    def set_flags(self, flags):
+        p, keep = _ptr(flags, np.uint8)
+        self._check(self.lib.lbmx_set_flags(self.h, p))
+
+    def init(self, rho, u, force=None):
+        pr, k1 = _ptr(rho, np.float32)
+        pu, k2 = _ptr(u, np.float32)
+        pf, k3 = _ptr(force, np.float32)
+        self._check(self.lib.lbmx_init_from_fields(self.h, pr, pu, pf))
+
+    def set_force_field(self, force):
+        pf, k = _ptr(force, np.float32)
+        self._check(self.lib.lbmx_set_force_field(self.h, pf))
+
+    def step(self, n=1, flags=STEP_STORE_MOMENTS):
+        self._check(self.lib.lbmx_step_ex(self.h, int(n), int(flags)))
+
+    def moments(self, rho=None, u=None):
+        """(rho[ny,nx], u[2,ny,nx], sums[3]) of the last stored step, as numpy."""
+        rho = np.empty((self.ny, self.nx), np.float32) if rho is None else rho
+        u = np.empty((2, self.ny, self.nx), np.float32) if u is None else u
+        s = (ctypes.c_double * 3)()
+        pr, _ = _ptr(rho, np.float32) if not isinstance(rho, np.ndarray) else (rho.ctypes.data, rho)
+        pu, _ = _ptr(u, np.float32) if not isinstance(u, np.ndarray) else (u.ctypes.data, u)
+        self._check(self.lib.lbmx_moments(self.h, pr, pu, s))
+        return rho, u, np.array(list(s))
+
+    def populations(self):
+        out = np.empty((9, self.ny, self.nx), np.float32)
+        self._check(self.lib.lbmx_get_populations(self.h, out.ctypes.data))
+        return out
+
+    def averages(self):
+        a = (ctypes.c_float * 3)()
+        self._check(self.lib.lbmx_averages(self.h, a))
+        return np.array(list(a))
+
+    def set_markers(self, xy):
+        p, k = _ptr(xy, np.float32)
+        n = int(np.asarray(xy).size // 2) if not hasattr(xy, "numel") else int(xy.numel() // 2)
+        self._check(self.lib.lbmx_ibm_set_markers(self.h, p, n))
+        self.nm = n
+
+    def marker_forces(self):
+        F = np.zeros(2 * max(self.nm, 1), np.float32)
+        dl = (ctypes.c_double * 2)()
+        self._check(self.lib.lbmx_ibm_forces(self.h, F.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), dl))
+        return F[: 2 * self.nm].reshape(2, self.nm), np.array(list(dl))
+
+    @property
+    def t(self):
+        return self.lib.lbmx_time(self.h)
+
+    def synchronize(self):
+        self._check(self.lib.lbmx_synchronize(self.h))

@@ -1,0 +1,189 @@
+/*
+ * lbmx.h -- C-ABI of the GB300 D2Q9 lattice Boltzmann engine (liblbmx.so).
+ *
+ * Plain C types only: a caller-owned opaque handle, plain pointers and sizes,
+ * integer status codes.  No call exits the process or resets the device
+ * (the reference's checkCudaErrors does both, src/util/utility.cu:4-12).
+ *
+ * Every pointer argument that carries a field may point to host memory
+ * (pageable or pinned) or to device memory of the handle's GPU; the engine
+ * copies with cudaMemcpyDefault.  Field layouts match the reference's
+ * shipped SoA form (src/core/lbm_constants.cuh:317-327): node = y*nx + x,
+ * vector fields as component planes (all x components, then all y).
+ *
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef LBMX_H
+#define LBMX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBMX_VERSION 1
+
+typedef int32_t lbmx_status;
+enum {
+    LBMX_OK = 0,
+    LBMX_ERR_INVALID_ARGUMENT = 1,
+    LBMX_ERR_OUT_OF_MEMORY = 2,
+    LBMX_ERR_CUDA = 3,
+    LBMX_ERR_INVALID_FLAGS = 4,   /* a flag the engine cannot apply (see lbmx_set_flags) */
+    LBMX_ERR_NOT_INITIALIZED = 5, /* lbmx_step before lbmx_init_from_fields */
+    LBMX_ERR_UNSUPPORTED = 6,
+    LBMX_ERR_NONFINITE = 7,       /* LBMX_STEP_CHECK_FINITE found NaN/Inf density */
+    LBMX_ERR_TOO_LARGE = 8
+};
+
+/* Collision operators: BGK<2>, MRT<2>, CM<2,NoAdapter>, CM<2,OptimalAdapter>
+ * (src/core/collision/BGK/BGK.cuh:13-51, MRT/MRT.cu:26-76, CM/CM.cuh:27-138,
+ *  adapters.cuh:16-22 and :48-111). */
+enum { LBMX_BGK = 0, LBMX_MRT = 1, LBMX_CM = 2, LBMX_CM_OPT = 3 };
+
+/* Population storage in HBM.  Offset forms store f_q - w_q in 16 bits; all
+ * arithmetic is FP32 in every form. */
+enum { LBMX_STORAGE_F32 = 0, LBMX_STORAGE_F16_OFFSET = 1, LBMX_STORAGE_BF16_OFFSET = 2 };
+
+/* Boundary flags.  0..12 keep the values of the reference's BC_flag
+ * (src/core/lbm_constants.cuh:376-396); 32.. are boundaries the reference
+ * does not have. */
+enum {
+    LBMX_FLUID = 0,
+    LBMX_BOUNCE_BACK = 1,            /* BounceBack<2>, bbDomainBoundary.cuh:14-50 */
+    LBMX_ZOU_HE_TOP = 2,             /* ZouHe::apply_top, zouHeInflow.cuh:42-56 */
+    LBMX_ZOU_HE_LEFT = 3,            /* ZouHe::apply_left, zouHeInflow.cuh:9-22 */
+    LBMX_ZOU_HE_TOP_LEFT_TOP_INFLOW = 4,  /* not implemented by the reference (asserts): rejected */
+    LBMX_ZOU_HE_TOP_RIGHT_TOP_INFLOW = 5, /* not implemented by the reference (asserts): rejected */
+    LBMX_CYLINDER = 6,               /* CylinderBoundary, cylinderBoundary.cuh:21-34 */
+    LBMX_ZG_OUTFLOW = 7,             /* ZG_OutflowBoundary<2>, zeroGradientOutflow.cuh:6-60 */
+    LBMX_PRESSURE_OUTLET = 8,        /* PressureOutlet, pressureOutlet.cuh:6-43 */
+    LBMX_REGULARIZED_INLET_TOP = 9,  /* RegularizedInlet::apply_top, regularizedInlet.cuh:13-70 */
+    LBMX_REGULARIZED_INLET_LEFT = 10,/* no 2-D dispatch in the reference: left untouched */
+    LBMX_REGULARIZED_BOUNCE_BACK = 11,        /* regularizedBounceBack.cuh:6-100 */
+    LBMX_REGULARIZED_BOUNCE_BACK_CORNER = 12, /* regularizedBounceBack.cuh:102-222 */
+    LBMX_MOVING_WALL_BB = 32,        /* half-way bounce-back with wall velocity (wall_ux, wall_uy) */
+    LBMX_ZOU_HE_PRESSURE_RIGHT = 33, /* Zou-He pressure outlet at x = nx-1, density rho_out */
+    LBMX_ZOU_HE_PARABOLIC_LEFT = 34, /* Zou-He velocity inlet at x = 0, parabolic profile of peak u_bc */
+    LBMX_HALFWAY_BB = 35             /* stationary half-way bounce-back */
+};
+
+/* Switches that reproduce the reference's as-shipped behaviour. */
+enum {
+    LBMX_QUIRK_REST_LAG = 1u << 0,   /* q=0 is never streamed (streaming.cu:9): f0 two steps back */
+    LBMX_QUIRK_ZOUHE_LEFT = 1u << 1, /* rho of the left Zou-He inlet uses f2 for f3 (zouHeInflow.cuh:15-16) */
+    LBMX_QUIRK_MRT_FORCE = 1u << 2,  /* MRT forcing moments in [jx,jy,qx,qy] order (MRT.cu:18-19) */
+    LBMX_QUIRK_IBM_2X2 = 1u << 3,    /* 2x2 stencil for the 4-point kernel (IBM_impl.cu:19-20) */
+    LBMX_QUIRK_IBM_CLAMP = 1u << 4,  /* drop negative IBM forces/velocities (IBM_impl.cuh:22-24, 42-44) */
+    LBMX_QUIRKS_REFERENCE = 0x1fu
+};
+
+/* lbmx_params.options */
+enum {
+    LBMX_OPTION_LAGGED_AVERAGES = 1u << 0 /* CM_OPT: use the previous step's grid averages (one pass) */
+};
+
+/* lbmx_step_ex flags */
+enum {
+    LBMX_STEP_STORE_MOMENTS = 1u << 0, /* last step stores rho, u and the FP64 sums */
+    LBMX_STEP_CHECK_FINITE = 1u << 1   /* last step flags non-finite densities */
+};
+
+/* Replaces the compile-time NX/NY/PERIODIC_* macros and the Scenario
+ * constexprs (viscosity/tau/omega, S[], u_max) the reference bakes in
+ * (src/defines.hpp:4-70, src/scenarios/scenario.cuh:36-59). */
+typedef struct lbmx_params {
+    int32_t nx, ny;
+    int32_t periodic_x, periodic_y;
+    int32_t op;          /* LBMX_BGK ... LBMX_CM_OPT */
+    int32_t storage;     /* LBMX_STORAGE_* */
+    uint32_t quirks;     /* LBMX_QUIRK_* */
+    uint32_t options;    /* LBMX_OPTION_* */
+    int32_t ibm_iters;   /* multi-direct iterations (reference ITER_MAX = 3) */
+    int32_t device;      /* CUDA device ordinal */
+    float omega;         /* BGK rate (Scenario::omega) */
+    float S[9];          /* MRT (M-row order) or CM (central-moment order) rates (Scenario::S) */
+    float u_bc;          /* Scenario::u_max for Zou-He / regularized / parabolic inlets */
+    float wall_ux, wall_uy; /* LBMX_MOVING_WALL_BB velocity */
+    float rho_out;       /* LBMX_ZOU_HE_PRESSURE_RIGHT density */
+    float ibm_ds;        /* marker weight on spread forces (reference: 1) */
+    float body_fx, body_fy; /* uniform body force when no force field is given */
+    void* stream;        /* cudaStream_t to run on; NULL: the handle creates one */
+} lbmx_params;
+
+typedef struct lbmx_handle lbmx_handle;
+
+/* Library version (LBMX_VERSION). */
+int32_t lbmx_version(void);
+
+/* Defaults: BGK, omega 1, FP32, no quirks, 3 IBM iterations, rho_out 1. */
+void lbmx_params_default(lbmx_params* p);
+
+/* Replaces LBM<2>::allocate<S>() + send_consts<S>() (src/core/lbm.cuh:92-125, :63-82). */
+lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out);
+
+/* Replaces ~LBM() / LBM::free() (src/core/lbm.cuh:127-140, :379-381). */
+void lbmx_destroy(lbmx_handle* h);
+
+/* Replaces LBM::setup_boundary_flags (src/core/boundaries/boundaries.cuh:170-197):
+ * nx*ny bytes of BC_flag values evaluated by the scenario's Boundary functor.
+ * Rejected (LBMX_ERR_INVALID_FLAGS): flags 4 and 5 (the reference asserts),
+ * values above 35, ZG / pressure / corner flags off the domain edge, and a
+ * pressure outlet at x = 0 (it reads node x-1). */
+lbmx_status lbmx_set_flags(lbmx_handle* h, const uint8_t* flags);
+
+/* Replaces init_kernel / LBM::init<S> (src/core/init/init.cuh:10-86): rho[n],
+ * u[2n] and the Init functor's force[2n] (NULL: the uniform body force of
+ * the params).  Populations start at the second-order equilibrium. */
+lbmx_status lbmx_init_from_fields(lbmx_handle* h, const float* rho, const float* u, const float* force);
+
+/* Replaces reset_forces_kernel / Init::apply_forces (macroscopics.cuh:13-48):
+ * the per-node force re-applied every step; NULL returns to the uniform
+ * body force of the params. */
+lbmx_status lbmx_set_force_field(lbmx_handle* h, const float* force);
+
+/* Replaces one pass of the reference loop body (src/main.cu:96-114):
+ * stream, boundaries, macroscopics, IBM, force correction, averages,
+ * equilibrium and collision, fused.  Stores moments on the last step. */
+lbmx_status lbmx_step(lbmx_handle* h, int32_t nsteps);
+lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags);
+
+/* Replaces LBM::update_macroscopics (src/core/lbm.cuh:148-154): the last
+ * stored step's density rho[n] and force-corrected velocity u[2n] (the
+ * reference's d_rho / d_u), and FP64 sums {rho, rho*ux, rho*uy}.  Any output
+ * pointer may be NULL. */
+lbmx_status lbmx_moments(lbmx_handle* h, float* rho, float* u, double* sums3);
+
+/* Post-collision populations of the last step, out[9*n], population planes
+ * in the reference's velocity order.  Slots whose value streamed out of a
+ * non-periodic domain in the last step hold NaN. */
+lbmx_status lbmx_get_populations(lbmx_handle* h, float* out);
+
+/* The grid averages {<rho>, <rho|u|>, <|Pi|>} of the last step (the
+ * reference's d_moment_avg, src/core/lbm.cu:19); computed for CM_OPT only. */
+lbmx_status lbmx_averages(lbmx_handle* h, float* avg3);
+
+/* Replaces IBMManager<2>::init_and_dispatch (src/IBM/IBMManager.cuh:54-109):
+ * n static markers, xy[2n] interleaved (the reference's IBMBody.points). */
+lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n);
+
+/* Marker forces of the last step, summed over the multi-direct iterations,
+ * force[2n] as planes, and drag/lift = -sum of marker forces (FP64). */
+lbmx_status lbmx_ibm_forces(lbmx_handle* h, float* force, double* drag_lift);
+
+/* Steps taken since lbmx_init_from_fields. */
+int64_t lbmx_time(lbmx_handle* h);
+
+/* Waits for the handle's stream. */
+lbmx_status lbmx_synchronize(lbmx_handle* h);
+
+/* Message of the last failed call on this handle ("" if none); with a NULL
+ * handle, the message of the last failed lbmx_create. */
+const char* lbmx_last_error(lbmx_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBMX_H */

@@ -1,0 +1,148 @@
+"""Seeded test cases shared by the parity tests, smoke() and bench.py.
+
+Each builder returns a dict with the lattice parameters (the same keys the
+engine binding and the oracle take), the boundary flags and the initial
+fields.  The configurations restate the reference's 2-D scenarios
+(src/scenarios/{taylorGreen,lidDrivenCavity,poiseuille,flowPastCylinder})
+at sizes the CPU oracle runs in seconds.
+"""
+import numpy as np
+
+BGK, MRT, CM, CM_OPT = 0, 1, 2, 3
+FLUID, BOUNCE_BACK, ZOU_HE_TOP, ZOU_HE_LEFT = 0, 1, 2, 3
+CYLINDER, ZG_OUTFLOW, PRESSURE_OUTLET, REGULARIZED_INLET_TOP = 6, 7, 8, 9
+REGULARIZED_BOUNCE_BACK, REGULARIZED_BOUNCE_BACK_CORNER = 11, 12
+MOVING_WALL_BB, ZOU_HE_PRESSURE_RIGHT, ZOU_HE_PARABOLIC_LEFT, HALFWAY_BB = 32, 33, 34, 35
+QUIRKS_REFERENCE = 0x1F
+
+
+def omega_of(nu):
+    """tau = 3 nu + 1/2 (viscosity_to_tau, src/core/lbm_constants.cuh:364-366)."""
+    return 1.0 / (3.0 * nu + 0.5)
+
+
+def mrt_S(omega):
+    """The reference's MRT rate set (taylorGreenScenario.cuh:32-42, lidDrivenCavityScenario.cuh:62-72)."""
+    return [0.0, 1.0, 1.4, 0.0, 1.2, 0.0, 1.9, omega, omega]
+
+
+def cm_S(omega):
+    """Central-moment rates of the reference scenarios (lidDrivenCavityScenario.cuh:50-60)."""
+    return [0.0, 0.0, 0.0, 1.0, omega, omega, 1.0, 1.0, 1.0]
+
+
+def S_for(op, omega):
+    return mrt_S(omega) if op == MRT else (cm_S(omega) if op in (CM, CM_OPT) else [omega] * 9)
+
+
+def base(nx, ny, op, nu, **kw):
+    om = omega_of(nu)
+    c = dict(nx=nx, ny=ny, op=op, omega=om, S=S_for(op, om), periodic=(False, False), quirks=0,
+             u_bc=0.0, wall_u=(0.0, 0.0), rho_out=1.0, flags=np.zeros((ny, nx), np.uint8),
+             rho=np.ones((ny, nx)), u=np.zeros((2, ny, nx)), force=None, markers=None)
+    c.update(kw)
+    return c
+
+
+def taylor_green(nx=64, ny=48, op=BGK, nu=0.01, u0=0.04, **kw):
+    """Decaying vortex, fully periodic: u = u0 sin kx cos ky, v = -u0 cos kx sin ky."""
+    kx, ky = 2 * np.pi / nx, 2 * np.pi / ny
+    X, Y = np.meshgrid(np.arange(nx), np.arange(ny))
+    ux = u0 * np.sin(kx * X) * np.cos(ky * Y)
+    uy = -u0 * (kx / ky) * np.cos(kx * X) * np.sin(ky * Y)
+    rho = 1.0 - 3.0 * (u0 ** 2 / 4.0) * (np.cos(2 * kx * X) + np.cos(2 * ky * Y))
+    return base(nx, ny, op, nu, periodic=(True, True), rho=rho, u=np.stack([ux, uy]), **kw)
+
+
+def cavity_regularized(nx=48, ny=40, op=BGK, nu=0.02, u_lid=0.1, **kw):
+    """The reference's lid-driven cavity flags (lidDrivenCavityFunctors.cuh:41-56)."""
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[0, :] = REGULARIZED_BOUNCE_BACK
+    fl[:, 0] = REGULARIZED_BOUNCE_BACK
+    fl[:, -1] = REGULARIZED_BOUNCE_BACK
+    fl[-1, :] = REGULARIZED_INLET_TOP
+    for y, x in ((0, 0), (0, nx - 1), (ny - 1, 0), (ny - 1, nx - 1)):
+        fl[y, x] = REGULARIZED_BOUNCE_BACK_CORNER
+    return base(nx, ny, op, nu, flags=fl, u_bc=u_lid, **kw)
+
+
+def cavity_moving_wall(nx=48, ny=40, op=MRT, nu=0.02, u_lid=0.1, **kw):
+    """Cavity with a half-way moving-wall lid and half-way bounce-back walls."""
+    fl = np.full((ny, nx), FLUID, np.uint8)
+    fl[0, :] = HALFWAY_BB
+    fl[:, 0] = HALFWAY_BB
+    fl[:, -1] = HALFWAY_BB
+    fl[-1, 1:-1] = MOVING_WALL_BB
+    return base(nx, ny, op, nu, flags=fl, wall_u=(u_lid, 0.0), **kw)
+
+
+def cavity_zouhe(nx=40, ny=32, op=BGK, nu=0.05, u_lid=0.05, **kw):
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[0, :] = BOUNCE_BACK
+    fl[:, 0] = BOUNCE_BACK
+    fl[:, -1] = BOUNCE_BACK
+    fl[-1, 1:-1] = ZOU_HE_TOP
+    return base(nx, ny, op, nu, flags=fl, u_bc=u_lid, **kw)
+
+
+def poiseuille(nx=64, ny=32, op=BGK, nu=1.0 / 6.0, u_max=0.05, **kw):
+    """Body-force channel, periodic x, bounce-back walls (poiseuilleFunctors.cuh:34-57)."""
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[0, :] = BOUNCE_BACK
+    fl[-1, :] = BOUNCE_BACK
+    F = np.zeros((2, ny, nx))
+    F[0] = 8.0 * nu * u_max / (ny * ny)
+    return base(nx, ny, op, nu, periodic=(True, False), flags=fl, force=F, **kw)
+
+
+def cylinder_markers(cx, cy, r, n):
+    """create_cylinder (src/IBM/IBM_generators.cu:5-25): n evenly spaced ring markers."""
+    a = 2 * np.pi / n
+    i = np.arange(n)
+    return np.stack([cx + r * np.cos(i * a), cy + r * np.sin(i * a)], axis=1).astype(np.float32)
+
+
+def channel(nx=96, ny=48, op=BGK, nu=0.04, u_in=0.05, inlet="zouhe", outlet="zg", markers=None, **kw):
+    """Flow past a cylinder channel (flowPastCylinderFunctors.cuh:62-93)."""
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[:, 0] = {"zouhe": ZOU_HE_LEFT, "parabolic": ZOU_HE_PARABOLIC_LEFT}[inlet]
+    fl[:, -1] = {"zg": ZG_OUTFLOW, "pressure": PRESSURE_OUTLET, "zouhe_p": ZOU_HE_PRESSURE_RIGHT}[outlet]
+    fl[0, :] = BOUNCE_BACK
+    fl[-1, :] = BOUNCE_BACK
+    return base(nx, ny, op, nu, flags=fl, u_bc=u_in, markers=markers, **kw)
+
+
+def random_state(c, seed=0, amp=0.02):
+    """Perturb the initial velocity with seeded noise (exercises every population)."""
+    rng = np.random.default_rng(seed)
+    c = dict(c)
+    c["u"] = c["u"] + amp * rng.standard_normal(c["u"].shape)
+    c["rho"] = c["rho"] * (1.0 + 0.01 * rng.standard_normal(c["rho"].shape))
+    return c
+
+
+def make_oracle(c, precision="f64"):
+    import oracle as O
+    o = O.Oracle(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], periodic=c["periodic"],
+                 quirks=c["quirks"], u_bc=c["u_bc"], wall_u=c["wall_u"], rho_out=c["rho_out"],
+                 precision=precision)
+    o.set_flags(c["flags"])
+    n = c["nx"] * c["ny"]
+    F = np.zeros(2 * n) if c["force"] is None else c["force"]
+    o.init(c["rho"], c["u"], F)
+    if c["markers"] is not None:
+        o.set_markers(c["markers"])
+    return o
+
+
+def make_lattice(c, storage=0, options=0):
+    import lbmx
+    L = lbmx.Lattice(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], periodic=c["periodic"],
+                     storage=storage, quirks=c["quirks"], options=options, u_bc=c["u_bc"],
+                     wall_u=c["wall_u"], rho_out=c["rho_out"])
+    L.set_flags(c["flags"])
+    L.init(np.asarray(c["rho"], np.float32), np.asarray(c["u"], np.float32),
+           None if c["force"] is None else np.asarray(c["force"], np.float32))
+    if c["markers"] is not None:
+        L.set_markers(c["markers"])
+    return L
