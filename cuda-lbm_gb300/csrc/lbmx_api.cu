@@ -9,6 +9,7 @@
 #include <cstring>
 #include <string>
 #include <unordered_map>
+#include <algorithm>
 #include <vector>
 
 #include "lbmx.h"
@@ -56,6 +57,16 @@ struct lbmx_handle {
     float* marker_u = nullptr;
     float* marker_rho = nullptr;
     float* marker_force = nullptr;
+    std::vector<int> patch_host;   // IBM patch node offsets
+    // work split of the step kernel
+    std::vector<uint8_t> flags_host;  // pitched copy of the flags (empty: all fluid)
+    int* special_units = nullptr;
+    uint32_t* special_bits = nullptr;
+    int nspecial = 0, special_blocks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
+    void* f_alloc = nullptr;  // population allocation including the guard elements
+    unsigned long long* tile_counter = nullptr;
+    unsigned int* done_counter = nullptr;
+    long long partial_cap = 0;
     char err[512] = {0};
 };
 
@@ -109,7 +120,88 @@ static StepArgs base_args(const lbmx_handle* h) {
     a.rho_out_bc = h->p.rho_out;
     a.body_fx = h->p.body_fx;
     a.body_fy = h->p.body_fy;
+    a.forced = (h->p.body_fx != 0.0f || h->p.body_fy != 0.0f || h->force != nullptr || h->nm > 0) ? 1 : 0;
+    a.special_units = h->special_units;
+    a.nspecial = h->nspecial;
+    a.special_blocks = h->special_blocks;
+    a.special_bits = h->special_bits;
+    a.tiles_x = h->tiles_x;
+    a.tiles_y = h->tiles_y;
+    a.num_ctas = h->num_ctas;
+    a.error_word = h->error_word;
+    a.tile_counter = h->tile_counter;
+    a.done_counter = h->done_counter;
     return a;
+}
+
+// Split the lattice between the two kinds of step-kernel CTAs: units (two
+// x-neighbouring nodes, x0 even) on the perimeter or holding a flagged or
+// IBM-forced node take the general path; the kernel finds perimeter units by
+// position and the others through a bit per unit.
+static lbmx_status rebuild_special(lbmx_handle* h) {
+    const Geometry& g = h->g;
+    const int units_per_row = g.pitch / 2;
+    std::vector<char> interior_special((size_t)g.ny * units_per_row, 0);
+    bool any_interior = false;
+    auto mark = [&](long long off) {
+        const int y = (int)(off / g.pitch), x0 = (int)(off % g.pitch) & ~1;
+        interior_special[(size_t)y * units_per_row + x0 / 2] = 1;
+    };
+    if (!h->flags_host.empty())
+        for (int y = 0; y < g.ny; y++)
+            for (int x = 0; x < g.nx; x++)
+                if (h->flags_host[(size_t)y * g.pitch + x]) mark((long long)y * g.pitch + x);
+    for (int off : h->patch_host) mark(off);
+    std::vector<int> units;
+    std::vector<uint32_t> bits(((size_t)g.ny * units_per_row + 31) / 32, 0u);
+    for (int y = 0; y < g.ny; y++)
+        for (int x0 = 0; x0 < g.nx; x0 += 2) {
+            const bool perim = y == 0 || y == g.ny - 1 || x0 == 0 || x0 + 1 >= g.nx - 1;
+            const size_t u = (size_t)y * units_per_row + x0 / 2;
+            if (perim || interior_special[u]) units.push_back(y * g.pitch + x0);
+            if (!perim && interior_special[u]) {
+                bits[u >> 5] |= 1u << (u & 31);
+                any_interior = true;
+            }
+        }
+    cudaFree(h->special_units);
+    cudaFree(h->special_bits);
+    h->special_units = nullptr;
+    h->special_bits = nullptr;
+    LBMX_CUDA(h, cudaMalloc((void**)&h->special_units, units.size() * sizeof(int)));
+    LBMX_CUDA(h, cudaMemcpy(h->special_units, units.data(), units.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (any_interior) {
+        LBMX_CUDA(h, cudaMalloc((void**)&h->special_bits, bits.size() * sizeof(uint32_t)));
+        LBMX_CUDA(h, cudaMemcpy(h->special_bits, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
+    h->nspecial = (int)units.size();
+    h->special_blocks = (h->nspecial + kStepThreads - 1) / kStepThreads;
+    h->tiles_x = (g.nx + kStageW - 1) / kStageW;
+    h->tiles_y = (g.ny - 2 + kStageH - 1) / kStageH;
+    // two persistent interior CTAs per SM walk the tiles
+    const long long tiles = (long long)h->tiles_x * h->tiles_y;
+    h->num_ctas = (int)std::min<long long>(tiles, 2LL * h->num_sms);
+    const long long blocks = h->special_blocks + h->num_ctas;
+    if (blocks > h->partial_cap) {
+        cudaFree(h->partials);
+        h->partials = nullptr;
+        LBMX_CUDA(h, cudaMalloc((void**)&h->partials, (size_t)blocks * 6 * sizeof(double)));
+        h->partial_cap = blocks;
+    }
+    return LBMX_OK;
+}
+
+// A staged tile whose copies never completed (bit 1 of the error word) is a
+// hard failure of the steps since the last check; the word is cleared.
+static lbmx_status check_pipeline(lbmx_handle* h) {
+    unsigned int w = 0;
+    LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (w & 2u) {
+        LBMX_CUDA(h, cudaMemsetAsync(h->error_word, 0, sizeof(w), h->stream));
+        return fail(h, LBMX_ERR_CUDA, "step kernel: a shared-memory staging wait gave up; results are invalid");
+    }
+    return LBMX_OK;
 }
 
 // parity and rest-population plane of step index s (1-based)
@@ -125,6 +217,7 @@ static void free_ibm(lbmx_handle* h) {
     h->patch_nodes = nullptr; h->sten_idx = nullptr; h->sten_w = nullptr;
     h->patch_rho = h->patch_u = h->marker_u = h->marker_rho = h->marker_force = h->ibm_force = nullptr;
     h->nm = h->npatch = 0;
+    h->patch_host.clear();
 }
 
 extern "C" {
@@ -150,10 +243,11 @@ void lbmx_destroy(lbmx_handle* h) {
     cudaSetDevice(h->p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_ibm(h);
-    cudaFree(h->f); cudaFree(h->flags); cudaFree(h->edge); cudaFree(h->aux);
+    cudaFree(h->f_alloc); cudaFree(h->flags); cudaFree(h->edge); cudaFree(h->aux);
     cudaFree(h->force); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
     cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums);
-    cudaFree(h->avg); cudaFree(h->error_word);
+    cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
+    cudaFree(h->tile_counter); cudaFree(h->done_counter);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     cudaSetDevice(cur);
     delete h;
@@ -180,15 +274,14 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     Geometry& g = h->g;
     g.nx = p->nx;
     g.ny = p->ny;
-    g.pitch = (p->nx + 63) / 64 * 64;
+    g.pitch = (p->nx + kStageW - 1) / kStageW * kStageW;  // whole staged tiles per row
     g.periodic_x = p->periodic_x ? 1 : 0;
     g.periodic_y = p->periodic_y ? 1 : 0;
     g.plane = (long long)g.ny * g.pitch;
     g.perimeter = 2 * g.nx + 2 * (g.ny - 2);
     h->nplanes = (p->quirks & LBMX_QUIRK_REST_LAG) ? 10 : 9;
     const long long n = (long long)g.nx * g.ny;
-    h->blocks = (long long)((g.nx + kBlockX - 1) / kBlockX) * ((g.ny + kBlockY - 1) / kBlockY);
-#define ALLOC(ptr, bytes)                                                                   \
+#define ALLOC(ptr, bytes)                                                                  \
     do {                                                                                    \
         cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));                               \
         if (e_ != cudaSuccess) {                                                            \
@@ -198,17 +291,21 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
             return LBMX_ERR_OUT_OF_MEMORY;                                                  \
         }                                                                                   \
     } while (0)
-    ALLOC(h->f, (size_t)h->nplanes * g.plane * elem_size(p->storage));
+    ALLOC(h->f_alloc, ((size_t)h->nplanes * g.plane + 2 * kGuardElems) * elem_size(p->storage));
+    h->f = static_cast<char*>(h->f_alloc) + (size_t)kGuardElems * elem_size(p->storage);
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+    if (h->num_sms < 1) h->num_sms = 1;
     ALLOC(h->edge, (size_t)2 * g.perimeter * 9 * sizeof(float));
     ALLOC(h->aux, (size_t)g.perimeter * 9 * sizeof(float));
     ALLOC(h->rho_out, (size_t)g.plane * sizeof(float));
     ALLOC(h->u_out, (size_t)2 * g.plane * sizeof(float));
     ALLOC(h->staging, (size_t)3 * n * sizeof(float));
-    ALLOC(h->partials, (size_t)h->blocks * 6 * sizeof(double));
     ALLOC(h->counter, sizeof(unsigned int));
     ALLOC(h->sums, 6 * sizeof(double));
     ALLOC(h->avg, 3 * sizeof(float));
     ALLOC(h->error_word, sizeof(unsigned int));
+    ALLOC(h->tile_counter, sizeof(unsigned long long));
+    ALLOC(h->done_counter, sizeof(unsigned int));
 #undef ALLOC
     if (p->stream) {
         h->stream = (cudaStream_t)p->stream;
@@ -224,11 +321,18 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     cudaMemsetAsync(h->sums, 0, 6 * sizeof(double), h->stream);
     cudaMemsetAsync(h->avg, 0, 3 * sizeof(float), h->stream);
     cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream);
+    cudaMemsetAsync(h->tile_counter, 0, sizeof(unsigned long long), h->stream);
+    cudaMemsetAsync(h->done_counter, 0, sizeof(unsigned int), h->stream);
     cudaMemsetAsync(h->aux, 0, (size_t)g.perimeter * 9 * sizeof(float), h->stream);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
         fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: initial clears failed");
         lbmx_destroy(h);
         return LBMX_ERR_CUDA;
+    }
+    if (rebuild_special(h) != LBMX_OK) {
+        fail(nullptr, LBMX_ERR_OUT_OF_MEMORY, "lbmx_create: %s", h->err);
+        lbmx_destroy(h);
+        return LBMX_ERR_OUT_OF_MEMORY;
     }
     *out = h;
     return LBMX_OK;
@@ -259,21 +363,24 @@ lbmx_status lbmx_set_flags(lbmx_handle* h, const uint8_t* flags) {
             if ((fl == LBMX_ZG_OUTFLOW || fl == LBMX_REGULARIZED_BOUNCE_BACK_CORNER) && edge) aux = true;
             if (fl == LBMX_PRESSURE_OUTLET) aux = true;
         }
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
     if (!any) {
         cudaFree(h->flags);
         h->flags = nullptr;
         h->has_aux_bc = false;
-        return LBMX_OK;
+        h->flags_host.clear();
+        return rebuild_special(h);
     }
     if (!h->flags) {
         cudaError_t e = cudaMalloc((void**)&h->flags, (size_t)g.plane);
         if (e != cudaSuccess) return fail(h, LBMX_ERR_OUT_OF_MEMORY, "lbmx_set_flags: cudaMalloc failed");
     }
-    LBMX_CUDA(h, cudaMemsetAsync(h->flags, 0, (size_t)g.plane, h->stream));
-    LBMX_CUDA(h, cudaMemcpy2DAsync(h->flags, g.pitch, hf.data(), g.nx, g.nx, g.ny, cudaMemcpyHostToDevice, h->stream));
-    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->flags_host.assign((size_t)g.plane, 0);
+    for (int y = 0; y < g.ny; y++)
+        memcpy(&h->flags_host[(size_t)y * g.pitch], &hf[(size_t)y * g.nx], g.nx);
+    LBMX_CUDA(h, cudaMemcpy(h->flags, h->flags_host.data(), (size_t)g.plane, cudaMemcpyHostToDevice));
     h->has_aux_bc = aux;
-    return LBMX_OK;
+    return rebuild_special(h);
 }
 
 static lbmx_status upload_force(lbmx_handle* h, const float* force) {
@@ -397,7 +504,7 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check) {
         // lagged CM_OPT: the averages of this step feed the next one
         a.avg_out = lagged ? h->avg : nullptr;
     }
-    if (check) a.error_word = h->error_word;
+    a.check_finite = check ? 1 : 0;
     LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->p.op, st); }));
     h->t = s;
     return LBMX_OK;
@@ -451,7 +558,7 @@ lbmx_status lbmx_moments(lbmx_handle* h, float* rho, float* u, double* sums3) {
         sums3[2] = s[2];
     }
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
-    return LBMX_OK;
+    return check_pipeline(h);
 }
 
 lbmx_status lbmx_get_populations(lbmx_handle* h, float* out) {
@@ -494,7 +601,7 @@ lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
     cudaSetDevice(h->p.device);
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
     free_ibm(h);
-    if (n == 0) return LBMX_OK;
+    if (n == 0) return rebuild_special(h);
     const Geometry& g = h->g;
     std::vector<float> hxy(2 * (size_t)n);
     LBMX_CUDA(h, cudaMemcpy(hxy.data(), xy, 2 * (size_t)n * sizeof(float), cudaMemcpyDefault));
@@ -551,7 +658,8 @@ lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
     LBMX_CUDA(h, cudaMemset(h->marker_force, 0, 2 * (size_t)n * sizeof(float)));
     LBMX_CUDA(h, cudaMemset(h->marker_u, 0, 2 * (size_t)n * sizeof(float)));
     LBMX_CUDA(h, cudaMemset(h->marker_rho, 0, (size_t)n * sizeof(float)));
-    return LBMX_OK;
+    h->patch_host = nodes;  // patch nodes read the IBM force: general path
+    return rebuild_special(h);
 }
 
 lbmx_status lbmx_ibm_forces(lbmx_handle* h, float* force, double* drag_lift) {
@@ -581,7 +689,7 @@ lbmx_status lbmx_synchronize(lbmx_handle* h) {
     if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_synchronize: NULL handle");
     cudaSetDevice(h->p.device);
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
-    return LBMX_OK;
+    return check_pipeline(h);
 }
 
 const char* lbmx_last_error(lbmx_handle* h) { return h ? h->err : g_create_err; }

@@ -2,6 +2,12 @@
 // storage conversion, AA-pattern population access, boundary conditions and
 // collision operators.  Every loop over populations is fully unrolled so the
 // nine populations of a node live in registers.
+//
+// The collision operators are templates over the arithmetic type R: `float`
+// for one node, `V2` for two neighbouring nodes carried in the two halves of
+// a register pair and computed with Blackwell's packed FP32x2 instructions
+// (FFMA2 / FADD2 / FMUL2), which halves the floating-point instruction count
+// of the interior path.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -27,6 +33,32 @@ __host__ __device__ constexpr float WQ(int q) {
     return q == 0 ? 4.0f / 9.0f : (q <= 4 ? 1.0f / 9.0f : 1.0f / 36.0f);
 }
 
+// ---------------------------------------------------------------- arithmetic
+// Two-node register pair with packed FP32x2 arithmetic (sm_100+).
+struct V2 {
+    float2 v;
+};
+__device__ __forceinline__ V2 splat(float s, V2) { return {make_float2(s, s)}; }
+__device__ __forceinline__ float splat(float s, float) { return s; }
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return {__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return {__ffma2_rn(b.v, make_float2(-1.f, -1.f), a.v)}; }
+__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return {__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ V2 operator*(float s, V2 b) { return {__fmul2_rn(make_float2(s, s), b.v)}; }
+__device__ __forceinline__ V2 operator-(V2 a) { return {make_float2(-a.v.x, -a.v.y)}; }
+__device__ __forceinline__ V2 fma(V2 a, V2 b, V2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ V2 fma(float a, V2 b, V2 c) { return {__ffma2_rn(make_float2(a, a), b.v, c.v)}; }
+__device__ __forceinline__ float fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ V2 vdiv(V2 a, V2 b) { return {make_float2(a.v.x / b.v.x, a.v.y / b.v.y)}; }
+__device__ __forceinline__ float vdiv(float a, float b) { return a / b; }
+__device__ __forceinline__ V2 vsqrt(V2 a) { return {make_float2(sqrtf(a.v.x), sqrtf(a.v.y))}; }
+__device__ __forceinline__ float vsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ V2 vmin(V2 a, float b) { return {make_float2(fminf(a.v.x, b), fminf(a.v.y, b))}; }
+__device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ V2 vpos_or(V2 a, float alt) {
+    return {make_float2(a.v.x > 0.f ? a.v.x : alt, a.v.y > 0.f ? a.v.y : alt)};
+}
+__device__ __forceinline__ float vpos_or(float a, float alt) { return a > 0.f ? a : alt; }
+
 // ---------------------------------------------------------------- storage
 // FP32 stores f itself; the 16-bit forms store the offset f - w_q, which is
 // O(|u|) instead of O(1) and so keeps 10 (FP16) or 7 (BF16) significant bits
@@ -35,32 +67,60 @@ template <typename T> struct Store;
 template <> struct Store<float> {
     static __device__ __forceinline__ float ld(const float* p, float) { return *p; }
     static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
+    static __device__ __forceinline__ float2 ld2(const float* p, float) { return *reinterpret_cast<const float2*>(p); }
+    static __device__ __forceinline__ void st2(float* p, float2 v, float) { *reinterpret_cast<float2*>(p) = v; }
 };
 template <> struct Store<__half> {
     static __device__ __forceinline__ float ld(const __half* p, float w) { return w + __half2float(*p); }
     static __device__ __forceinline__ void st(__half* p, float v, float w) { *p = __float2half_rn(v - w); }
+    static __device__ __forceinline__ float2 ld2(const __half* p, float w) {
+        const float2 d = __half22float2(*reinterpret_cast<const __half2*>(p));
+        return make_float2(d.x + w, d.y + w);
+    }
+    static __device__ __forceinline__ void st2(__half* p, float2 v, float w) {
+        *reinterpret_cast<__half2*>(p) = __float22half2_rn(make_float2(v.x - w, v.y - w));
+    }
 };
 template <> struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float w) { return w + __bfloat162float(*p); }
     static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
+    static __device__ __forceinline__ float2 ld2(const __nv_bfloat16* p, float w) {
+        const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+        return make_float2(d.x + w, d.y + w);
+    }
+    static __device__ __forceinline__ void st2(__nv_bfloat16* p, float2 v, float w) {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn(make_float2(v.x - w, v.y - w));
+    }
 };
 
 __device__ __forceinline__ bool on_edge(const Geometry& g, int x, int y) {
     return x == 0 || y == 0 || x == g.nx - 1 || y == g.ny - 1;
 }
 
-// Post-stream populations of node (x, y) for the current step.
+__device__ __forceinline__ bool is_halfway(uint8_t fl) { return fl == LBMX_MOVING_WALL_BB || fl == LBMX_HALFWAY_BB; }
+
+// Ladd's moving-wall term 2 w_q rho_w (c_q . u_w) / cs^2 with rho_w = 1
+__device__ __forceinline__ float wall_term(const StepArgs& a, int q, uint8_t fl) {
+    if (fl != LBMX_MOVING_WALL_BB) return 0.0f;
+    return 6.0f * WQ(q) * ((float)CX(q) * a.wall_ux + (float)CY(q) * a.wall_uy);
+}
+
+// Post-stream populations of node (x, y) for the current step (general path).
 // parity 1: f_q(x) sits in slot OPP(q) of the upstream node x - c_q;
-// parity 0: it sits in slot q of x itself.  Upstream nodes outside a
-// non-periodic domain read the edge store (bit q of *outmask set).
+// parity 0: it sits in slot q of x itself.  An upstream node outside a
+// non-periodic domain sets bit q of *outmask; the value then comes from the
+// edge store (what the reference's ping-pong buffers hold there, two steps
+// old) or, on a half-way bounce-back node, from the node's own slot q, where
+// the previous step left its reflected outgoing population.
 template <typename T>
-__device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y, float f[9],
+__device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y, uint8_t fl, float f[9],
                                                  unsigned* outmask) {
     const Geometry& g = a.g;
     const T* F = static_cast<const T*>(a.f);
     const long long row = (long long)y * g.pitch;
     f[0] = Store<T>::ld(F + a.rest_plane * g.plane + row + x, WQ(0));
     const bool edge = on_edge(g, x, y);
+    const bool hw = is_halfway(fl);
     const float* E = a.edge + ((long long)a.parity * g.perimeter + (edge ? edge_index(x, y, g.nx, g.ny) : 0)) * 9;
     unsigned m = 0;
 #pragma unroll
@@ -76,8 +136,13 @@ __device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y
             else out = true;
         }
         if (out) {
-            f[q] = E[q];
             m |= 1u << q;
+            if (hw) {
+                const float v = Store<T>::ld(F + q * g.plane + row + x, WQ(q));
+                f[q] = a.parity ? v - wall_term(a, OPP(q), fl) : v;
+            } else {
+                f[q] = E[q];
+            }
         } else if (a.parity) {
             f[q] = Store<T>::ld(F + OPP(q) * g.plane + (long long)sy * g.pitch + sx, WQ(q));
         } else {
@@ -87,16 +152,18 @@ __device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y
     *outmask = m;
 }
 
-// Write the post-collision populations of node (x, y).
-// parity 1: f*_q goes to slot q of the downstream node x + c_q (dropped when
-// that node lies outside a non-periodic domain, as the reference's push
-// skips it, streaming.cu:20-21); parity 0: to slot OPP(q) of x.
+// Write the post-collision populations of node (x, y) (general path).
+// parity 1: f*_q goes to slot q of the downstream node x + c_q -- dropped
+// when that node lies outside a non-periodic domain, as the reference's push
+// skips it (streaming.cu:20-21), or, on a half-way node, reflected into the
+// node's own free slot OPP(q); parity 0: to slot OPP(q) of x.
 template <typename T>
 __device__ __forceinline__ void store_post_collision(const StepArgs& a, int x, int y, const float f[9],
                                                      unsigned outmask, uint8_t fl) {
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
     const long long row = (long long)y * g.pitch;
+    const bool hw = is_halfway(fl);
     Store<T>::st(F + a.rest_plane * g.plane + row + x, f[0], WQ(0));
 #pragma unroll
     for (int q = 1; q < 9; q++) {
@@ -112,30 +179,16 @@ __device__ __forceinline__ void store_post_collision(const StepArgs& a, int x, i
                 else out = true;
             }
             if (!out) Store<T>::st(F + q * g.plane + (long long)dy * g.pitch + dx, f[q], WQ(q));
+            else if (hw) Store<T>::st(F + OPP(q) * g.plane + row + x, f[q] - wall_term(a, q, fl), WQ(q));
         } else {
             Store<T>::st(F + OPP(q) * g.plane + row + x, f[q], WQ(q));
         }
     }
-    if (outmask) {
-        const int e = edge_index(x, y, g.nx, g.ny);
-        float* E = a.edge + ((long long)a.parity * g.perimeter + e) * 9;
-        if (fl == LBMX_MOVING_WALL_BB || fl == LBMX_HALFWAY_BB) {
-            // half-way bounce-back: a population leaving through the wall
-            // (its reverse has an outside upstream node) comes back reversed
-            // next step, with Ladd's term -2 w rho_w c.u_w / cs^2, rho_w = 1
-            float* En = a.edge + ((long long)(a.parity ^ 1) * g.perimeter + e) * 9;
-            const bool moving = fl == LBMX_MOVING_WALL_BB;
+    if (outmask && !hw) {
+        float* E = a.edge + ((long long)a.parity * g.perimeter + edge_index(x, y, g.nx, g.ny)) * 9;
 #pragma unroll
-            for (int q = 1; q < 9; q++)
-                if (outmask & (1u << OPP(q))) {
-                    const float cu = (float)CX(q) * a.wall_ux + (float)CY(q) * a.wall_uy;
-                    En[OPP(q)] = f[q] - (moving ? 6.0f * WQ(q) * cu : 0.0f);
-                }
-        } else {
-#pragma unroll
-            for (int q = 1; q < 9; q++)
-                if (outmask & (1u << q)) E[q] = f[q];
-        }
+        for (int q = 1; q < 9; q++)
+            if (outmask & (1u << q)) E[q] = f[q];
     }
 }
 
@@ -322,8 +375,6 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
         if ((x == 0 || x == g.nx - 1) && (y == 0 || y == g.ny - 1))
             bc_reg_corner(g, f, x, y, a.aux[(long long)edge_index(x, y, g.nx, g.ny) * 9]);
         break;
-    case LBMX_MOVING_WALL_BB:
-    case LBMX_HALFWAY_BB: break;  // applied by store_post_collision
     case LBMX_ZOU_HE_PRESSURE_RIGHT: bc_zouhe_pressure_right(f, a.rho_out_bc); break;
     case LBMX_ZOU_HE_PARABOLIC_LEFT: {
         float h = (float)(g.ny - 1);
@@ -331,24 +382,40 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
         bc_zouhe_left(f, ux, false);
         break;
     }
-    default: break;  // the reference leaves unknown flags alone
+    default: break;  // half-way walls act in load/store; unknown flags are left alone as the reference does
     }
 }
 
 // ---------------------------------------------------------------- collision
+// All operators take the post-stream (post-boundary) populations f, the
+// density, the force-corrected velocity and the force, and overwrite f with
+// the post-collision populations.
 
 // BGK<2>::apply with Guo forcing -- BGK.cuh:15-39
-__device__ __forceinline__ void collide_bgk(float f[9], float rho, float ux, float uy, float Fx, float Fy,
-                                            float omega) {
-    const float uu = ux * ux + uy * uy;
+template <typename R>
+__device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R Fy, float omega, bool forced) {
+    const R uu = fma(ux, ux, uy * uy);
+    const R one = splat(1.0f, ux);
+    const R base = fma(splat(-1.5f, ux), uu, one);
     const float pref = 1.0f - 0.5f * omega;
 #pragma unroll
     for (int q = 0; q < 9; q++) {
         const float cx = (float)CX(q), cy = (float)CY(q);
-        const float cu = cx * ux + cy * uy;
-        const float feq = WQ(q) * rho * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
-        const float ft = WQ(q) * pref * ((3.0f * (cx - ux) + 9.0f * cu * cx) * Fx + (3.0f * (cy - uy) + 9.0f * cu * cy) * Fy);
-        f[q] = f[q] - omega * (f[q] - feq) + ft;
+        R cu;
+        if (CX(q) == 0) cu = cy * uy;
+        else if (CY(q) == 0) cu = cx * ux;
+        else cu = fma(cx, ux, cy * uy);
+        // feq = w rho (1 + 3cu + 4.5cu^2 - 1.5uu)
+        const R br = fma(cu, fma(splat(4.5f, ux), cu, splat(3.0f, ux)), base);
+        const R feq = (WQ(q) * rho) * br;
+        R fn = fma(splat(omega, ux), feq - f[q], f[q]);
+        if (forced) {
+            // w (1 - omega/2) [ (3(c - u) + 9 (c.u) c) . F ]
+            const R gx = fma(splat(9.0f * cx, ux), cu, 3.0f * (splat(cx, ux) - ux));
+            const R gy = fma(splat(9.0f * cy, ux), cu, 3.0f * (splat(cy, ux) - uy));
+            fn = fma(splat(WQ(q) * pref, ux), fma(gx, Fx, gy * Fy), fn);
+        }
+        f[q] = fn;
     }
 }
 
@@ -356,134 +423,158 @@ __device__ __forceinline__ void collide_bgk(float f[9], float rho, float ux, flo
 // [rho, e, eps, jx, qx, jy, qy, pxx, pxy]; the equilibrium moments are
 // M f_eq of the second-order equilibrium in closed form; the back transform
 // uses M^-1 = M^T diag(1/|row|^2) (the rows are orthogonal).
-__device__ __forceinline__ void collide_mrt(float f[9], float rho, float ux, float uy, float Fx, float Fy,
-                                            const float S[9], bool force_quirk) {
-    const float axis = f[1] + f[2] + f[3] + f[4];
-    const float diag = f[5] + f[6] + f[7] + f[8];
-    float m[9];
-    m[0] = f[0] + axis + diag;
-    m[1] = -4.0f * f[0] - axis + 2.0f * diag;
-    m[2] = 4.0f * f[0] - 2.0f * axis + diag;
-    m[3] = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
-    m[4] = -2.0f * (f[1] - f[3]) + f[5] - f[6] - f[7] + f[8];
-    m[5] = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
-    m[6] = -2.0f * (f[2] - f[4]) + f[5] + f[6] - f[7] - f[8];
-    m[7] = f[1] - f[2] + f[3] - f[4];
-    m[8] = f[5] - f[6] + f[7] - f[8];
-    const float uu = ux * ux + uy * uy;
-    float meq[9];
-    meq[0] = rho;
-    meq[1] = rho * (-2.0f + 3.0f * uu);
-    meq[2] = rho * (1.0f - 3.0f * uu);
-    meq[3] = rho * ux;
-    meq[4] = -rho * ux;
-    meq[5] = rho * uy;
-    meq[6] = -rho * uy;
-    meq[7] = rho * (ux * ux - uy * uy);
-    meq[8] = rho * ux * uy;
-    const float fu = Fx * ux + Fy * uy;
-    float Fm[9];
-    Fm[0] = 0.0f;
-    Fm[1] = 6.0f * fu;
-    Fm[2] = -6.0f * fu;
-    Fm[3] = Fx;
-    Fm[4] = force_quirk ? Fy : -Fx;
-    Fm[5] = force_quirk ? -Fx : Fy;
-    Fm[6] = -Fy;
-    Fm[7] = 2.0f * (Fx * ux - Fy * uy);
-    Fm[8] = Fx * uy + Fy * ux;
-    float a[9];
+template <typename R>
+__device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R Fy, const float S[9],
+                                            bool force_quirk, bool forced) {
+    const R axis = (f[1] + f[2]) + (f[3] + f[4]);
+    const R diag = (f[5] + f[6]) + (f[7] + f[8]);
+    const R d13 = f[1] - f[3], d24 = f[2] - f[4];
+    const R d58 = f[5] + f[8], d67 = f[6] + f[7];
+    const R d56 = f[5] + f[6], d78 = f[7] + f[8];
+    R m[9];
+    m[1] = fma(splat(2.0f, rho), diag, fma(splat(-4.0f, rho), f[0], -axis));
+    m[2] = fma(splat(4.0f, rho), f[0], fma(splat(-2.0f, rho), axis, diag));
+    m[3] = d13 + (d58 - d67);
+    m[4] = fma(splat(-2.0f, rho), d13, d58 - d67);
+    m[5] = d24 + (d56 - d78);
+    m[6] = fma(splat(-2.0f, rho), d24, d56 - d78);
+    m[7] = (f[1] + f[3]) - (f[2] + f[4]);
+    m[8] = (f[5] + f[7]) - (f[6] + f[8]);
+    const R uu = fma(ux, ux, uy * uy);
+    const R rux = rho * ux, ruy = rho * uy;
+    R meq[9];
+    meq[1] = rho * fma(splat(3.0f, rho), uu, splat(-2.0f, rho));
+    meq[2] = rho * fma(splat(-3.0f, rho), uu, splat(1.0f, rho));
+    meq[3] = rux;
+    meq[4] = -rux;
+    meq[5] = ruy;
+    meq[6] = -ruy;
+    meq[7] = rho * fma(ux, ux, -(uy * uy));
+    meq[8] = rux * uy;
+    // post-collision moments m - S (m - m_eq), scaled by 1/|row|^2; the density
+    // moment is conserved exactly (m_eq = m)
     const float inv_norm[9] = {1.0f / 9.0f, 1.0f / 36.0f, 1.0f / 36.0f, 1.0f / 6.0f, 1.0f / 12.0f,
                                1.0f / 6.0f, 1.0f / 12.0f, 0.25f, 0.25f};
+    R a[9];
+    a[0] = (1.0f / 9.0f) * rho;
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
-        const float mp = m[k] - S[k] * (m[k] - meq[k]) + (1.0f - 0.5f * S[k]) * Fm[k];
-        a[k] = mp * inv_norm[k];
+    for (int k = 1; k < 9; k++) a[k] = inv_norm[k] * fma(splat(-S[k], rho), m[k] - meq[k], m[k]);
+    if (forced) {
+        // (1 - S/2) F in moment space (MRT.cu:4-24, Silva & Semiao 2012)
+        const R fu = fma(Fx, ux, Fy * uy);
+        R Fm[9];
+        Fm[1] = 6.0f * fu;
+        Fm[2] = -6.0f * fu;
+        Fm[3] = Fx;
+        Fm[4] = force_quirk ? Fy : -Fx;
+        Fm[5] = force_quirk ? -Fx : Fy;
+        Fm[6] = -Fy;
+        Fm[7] = 2.0f * fma(Fx, ux, -(Fy * uy));
+        Fm[8] = fma(Fx, uy, Fy * ux);
+#pragma unroll
+        for (int k = 1; k < 9; k++) a[k] = fma(splat(inv_norm[k] * (1.0f - 0.5f * S[k]), rho), Fm[k], a[k]);
     }
-    const float base_axis = a[0] - a[1] - 2.0f * a[2];
-    const float base_diag = a[0] + 2.0f * a[1] + a[2];
-    f[0] = a[0] - 4.0f * a[1] + 4.0f * a[2];
-    f[1] = base_axis + a[3] - 2.0f * a[4] + a[7];
-    f[2] = base_axis + a[5] - 2.0f * a[6] - a[7];
-    f[3] = base_axis - a[3] + 2.0f * a[4] + a[7];
-    f[4] = base_axis - a[5] + 2.0f * a[6] - a[7];
-    const float px = a[3] + a[4], py = a[5] + a[6];
-    f[5] = base_diag + px + py + a[8];
-    f[6] = base_diag - px + py - a[8];
-    f[7] = base_diag - px - py + a[8];
-    f[8] = base_diag + px - py - a[8];
+    const R base_axis = a[0] - fma(splat(2.0f, rho), a[2], a[1]);
+    const R base_diag = a[0] + fma(splat(2.0f, rho), a[1], a[2]);
+    f[0] = fma(splat(4.0f, rho), a[2] - a[1], a[0]);
+    const R ax = fma(splat(-2.0f, rho), a[4], a[3]);
+    const R ay = fma(splat(-2.0f, rho), a[6], a[5]);
+    f[1] = base_axis + (ax + a[7]);
+    f[3] = base_axis - (ax - a[7]);
+    f[2] = base_axis + (ay - a[7]);
+    f[4] = base_axis - (ay + a[7]);
+    const R px = a[3] + a[4], py = a[5] + a[6];
+    f[5] = base_diag + ((px + py) + a[8]);
+    f[6] = base_diag + ((py - px) - a[8]);
+    f[7] = base_diag - ((px + py) - a[8]);
+    f[8] = base_diag + ((px - py) - a[8]);
 }
 
 // CM<2,Adapter>::apply -- CM.cuh:27-138.  Central moments about the
 // force-corrected velocity, De Rosis (2019) forcing, relaxation with S[i]
-// or the adapter rate for i > 5, back transform through raw moments.
-// `hor` is the higher-order rate (CM_OPT) or negative for NoAdapter.
-__device__ __forceinline__ void collide_cm(float f[9], float rho, float ux, float uy, float Fx, float Fy,
-                                           const float S[9], float hor) {
-    // raw moments of f
-    const float m10 = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
-    const float m01 = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
-    const float m20 = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
-    const float m02 = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
-    const float m11 = f[5] - f[6] + f[7] - f[8];
-    const float m21 = f[5] + f[6] - f[7] - f[8];
-    const float m12 = f[5] - f[6] - f[7] + f[8];
-    const float m22 = f[5] + f[6] + f[7] + f[8];
-    const float m00 = rho;
+// or the adapter rate `hor` for i > 5 (NoAdapter: use_hor = false), back
+// transform through raw moments (binomial shift) and the raw-moment basis
+// of D2Q9, the same linear map as the reference's closed-form T^-1(u).
+template <typename R>
+__device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy, const float S[9], R hor,
+                                           bool use_hor) {
+    const R m10 = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
+    const R m01 = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
+    const R m22 = (f[5] + f[6]) + (f[7] + f[8]);
+    const R m20 = (f[1] + f[3]) + m22;
+    const R m02 = (f[2] + f[4]) + m22;
+    const R m11 = (f[5] + f[7]) - (f[6] + f[8]);
+    const R m21 = (f[5] + f[6]) - (f[7] + f[8]);
+    const R m12 = (f[5] + f[8]) - (f[6] + f[7]);
+    const R ux2 = ux * ux, uy2 = uy * uy, uxy = ux * uy;
+    const R two = splat(2.0f, rho);
     // central moments kappa_ab = sum f (cx-ux)^a (cy-uy)^b
-    const float ux2 = ux * ux, uy2 = uy * uy;
-    const float k10 = m10 - ux * m00;
-    const float k01 = m01 - uy * m00;
-    const float k20 = m20 - 2.0f * ux * m10 + ux2 * m00;
-    const float k02 = m02 - 2.0f * uy * m01 + uy2 * m00;
-    const float k11 = m11 - ux * m01 - uy * m10 + ux * uy * m00;
-    const float k21 = m21 - 2.0f * ux * m11 - uy * m20 + ux2 * m01 + 2.0f * ux * uy * m10 - ux2 * uy * m00;
-    const float k12 = m12 - 2.0f * uy * m11 - ux * m02 + uy2 * m10 + 2.0f * ux * uy * m01 - ux * uy2 * m00;
-    const float k22 = m22 - 2.0f * ux * m12 - 2.0f * uy * m21 + ux2 * m02 + uy2 * m20 + 4.0f * ux * uy * m11
-                    - 2.0f * ux * uy2 * m10 - 2.0f * ux2 * uy * m01 + ux2 * uy2 * m00;
+    const R k10 = fma(-ux, rho, m10);
+    const R k01 = fma(-uy, rho, m01);
+    const R k20 = fma(ux2, rho, fma(-two * ux, m10, m20));
+    const R k02 = fma(uy2, rho, fma(-two * uy, m01, m02));
+    const R k11 = fma(uxy, rho, fma(-ux, m01, fma(-uy, m10, m11)));
+    const R k21 = fma(-(ux2 * uy), rho, fma(two * uxy, m10, fma(ux2, m01, fma(-uy, m20, fma(-two * ux, m11, m21)))));
+    const R k12 = fma(-(ux * uy2), rho, fma(two * uxy, m01, fma(uy2, m10, fma(-ux, m02, fma(-two * uy, m11, m12)))));
+    const R k22 = fma(ux2 * uy2, rho,
+                      fma(-two * (ux2 * uy), m01,
+                          fma(-two * (ux * uy2), m10,
+                              fma(splat(4.0f, rho) * uxy, m11,
+                                  fma(uy2, m20, fma(ux2, m02, fma(-two * uy, m21, fma(-two * ux, m12, m22))))))));
     const float cs2 = 1.0f / 3.0f;
-    float k[9] = {rho, k10, k01, k20 + k02, k20 - k02, k11, k21, k12, k22};
-    const float keq[9] = {rho, 0.f, 0.f, 2.0f * rho * cs2, 0.f, 0.f, 0.f, 0.f, rho * cs2 * cs2};
-    const float Fc[9] = {0.f, Fx, Fy, 0.f, 0.f, 0.f, Fy * cs2, Fx * cs2, 0.f};
-#pragma unroll
-    for (int i = 0; i < 9; i++) {
-        const float s = (hor >= 0.0f && i > 5) ? hor : S[i];
-        k[i] = k[i] - s * (k[i] - keq[i]) + (1.0f - 0.5f * s) * Fc[i];
-    }
+    // relaxation k - s (k - k_eq) + (1 - s/2) F with k_eq = [rho, 0, 0,
+    // 2 rho cs2, 0, 0, 0, 0, rho cs2^2] and F = [0, Fx, Fy, 0, 0, 0, Fy cs2, Fx cs2, 0]
+    const R s3 = splat(S[3], rho), s4 = splat(S[4], rho), s5 = splat(S[5], rho);
+    const R s6 = use_hor ? hor : splat(S[6], rho);
+    const R s7 = use_hor ? hor : splat(S[7], rho);
+    const R s8 = use_hor ? hor : splat(S[8], rho);
+    const R one = splat(1.0f, rho), half = splat(0.5f, rho);
+    const R c10 = fma(splat(-S[1], rho), k10, k10) + (1.0f - 0.5f * S[1]) * Fx;
+    const R c01 = fma(splat(-S[2], rho), k01, k01) + (1.0f - 0.5f * S[2]) * Fy;
+    const R ksum = k20 + k02, kdiff = k20 - k02;
+    const R t3 = fma(-s3, ksum - (2.0f * cs2) * rho, ksum);
+    const R t4 = fma(-s4, kdiff, kdiff);
+    const R c11 = fma(-s5, k11, k11);
+    const R c21 = fma(fma(-half, s6, one), cs2 * Fy, fma(-s6, k21, k21));
+    const R c12 = fma(fma(-half, s7, one), cs2 * Fx, fma(-s7, k12, k12));
+    const R c22 = fma(-s8, k22 - (cs2 * cs2) * rho, k22);
+    const R c20 = 0.5f * (t3 + t4), c02 = 0.5f * (t3 - t4);
+    const R c00 = rho;
     // back to raw moments (binomial shift by +u), then to populations
-    const float c00 = k[0], c10 = k[1], c01 = k[2];
-    const float c20 = 0.5f * (k[3] + k[4]), c02 = 0.5f * (k[3] - k[4]);
-    const float c11 = k[5], c21 = k[6], c12 = k[7], c22 = k[8];
-    const float r10 = c10 + ux * c00;
-    const float r01 = c01 + uy * c00;
-    const float r20 = c20 + 2.0f * ux * c10 + ux2 * c00;
-    const float r02 = c02 + 2.0f * uy * c01 + uy2 * c00;
-    const float r11 = c11 + ux * c01 + uy * c10 + ux * uy * c00;
-    const float r21 = c21 + 2.0f * ux * c11 + uy * c20 + ux2 * c01 + 2.0f * ux * uy * c10 + ux2 * uy * c00;
-    const float r12 = c12 + 2.0f * uy * c11 + ux * c02 + uy2 * c10 + 2.0f * ux * uy * c01 + ux * uy2 * c00;
-    const float r22 = c22 + 2.0f * ux * c12 + 2.0f * uy * c21 + ux2 * c02 + uy2 * c20 + 4.0f * ux * uy * c11
-                    + 2.0f * ux * uy2 * c10 + 2.0f * ux2 * uy * c01 + ux2 * uy2 * c00;
-    f[0] = c00 - r20 - r02 + r22;
-    f[1] = 0.5f * (r10 + r20 - r12 - r22);
-    f[3] = 0.5f * (-r10 + r20 + r12 - r22);
-    f[2] = 0.5f * (r01 + r02 - r21 - r22);
-    f[4] = 0.5f * (-r01 + r02 + r21 - r22);
-    f[5] = 0.25f * (r11 + r21 + r12 + r22);
-    f[6] = 0.25f * (-r11 + r21 - r12 + r22);
-    f[7] = 0.25f * (r11 - r21 - r12 + r22);
-    f[8] = 0.25f * (-r11 - r21 + r12 + r22);
+    const R r10 = fma(ux, c00, c10);
+    const R r01 = fma(uy, c00, c01);
+    const R r20 = fma(ux2, c00, fma(two * ux, c10, c20));
+    const R r02 = fma(uy2, c00, fma(two * uy, c01, c02));
+    const R r11 = fma(uxy, c00, fma(ux, c01, fma(uy, c10, c11)));
+    const R r21 = fma(ux2 * uy, c00, fma(two * uxy, c10, fma(ux2, c01, fma(uy, c20, fma(two * ux, c11, c21)))));
+    const R r12 = fma(ux * uy2, c00, fma(two * uxy, c01, fma(uy2, c10, fma(ux, c02, fma(two * uy, c11, c12)))));
+    const R r22 = fma(ux2 * uy2, c00,
+                      fma(two * (ux2 * uy), c01,
+                          fma(two * (ux * uy2), c10,
+                              fma(splat(4.0f, rho) * uxy, c11,
+                                  fma(uy2, c20, fma(ux2, c02, fma(two * uy, c21, fma(two * ux, c12, c22))))))));
+    f[0] = (c00 - (r20 + r02)) + r22;
+    f[1] = 0.5f * ((r10 + r20) - (r12 + r22));
+    f[3] = 0.5f * ((r20 + r12) - (r10 + r22));
+    f[2] = 0.5f * ((r01 + r02) - (r21 + r22));
+    f[4] = 0.5f * ((r02 + r21) - (r01 + r22));
+    f[5] = 0.25f * ((r11 + r21) + (r12 + r22));
+    f[6] = 0.25f * ((r21 + r22) - (r11 + r12));
+    f[7] = 0.25f * ((r11 + r22) - (r21 + r12));
+    f[8] = 0.25f * ((r12 + r22) - (r11 + r21));
 }
 
 // OptimalAdapter::compute_higher_order_relaxation -- adapters.cuh:48-111
 // (Li et al. 2020 regression, theta* = (0.0003, -0.00775, 0.00016, 0.0087)).
-__device__ __forceinline__ float optimal_rate(float rho, float jmag, float pimag, const float* avg) {
-    float ts = 0.0003f * (rho / avg[0]);
-    ts += -0.00775f * (jmag / avg[1]);
-    ts += 0.00016f * (pimag / avg[2]);
-    ts += 0.0087f;
-    ts = ts > 0.0f ? ts : 0.005f;
-    ts = fminf(ts, 1.5f);
-    return 1.0f / (3.0f * ts + 0.5f);
+template <typename R>
+__device__ __forceinline__ R optimal_rate(R rho, R jmag, R pimag, const float* avg) {
+    R ts = (0.0003f / avg[0]) * rho;
+    ts = fma(splat(-0.00775f / avg[1], rho), jmag, ts);
+    ts = fma(splat(0.00016f / avg[2], rho), pimag, ts);
+    ts = ts + splat(0.0087f, rho);
+    ts = vpos_or(ts, 0.005f);
+    ts = vmin(ts, 1.5f);
+    return vdiv(splat(1.0f, rho), fma(splat(3.0f, rho), ts, splat(0.5f, rho)));
 }
 
 }  // namespace lbmx

@@ -40,7 +40,8 @@ struct StepArgs {
     unsigned int* counter;   // last-block-done counter for the sums
     double* sums;            // [6] final sums
     float* avg_out;          // averages produced by the last block (lagged CM_OPT / pre-pass)
-    unsigned int* error_word;// non-finite detection (nullptr: off)
+    unsigned int* error_word;// bit 0: non-finite density seen, bit 1: a staging wait gave up
+    int check_finite;        // look for non-finite densities this step
     uint32_t quirks;
     int parity;              // step index & 1; 1 = neighbour-access phase
     int rest_plane;          // plane that holds f0 this step (0 or 9)
@@ -48,6 +49,16 @@ struct StepArgs {
     float S[9];
     float u_bc, wall_ux, wall_uy, rho_out_bc;
     float body_fx, body_fy;
+    int forced;              // any non-zero force (body, field or IBM)
+    // work split of the step kernel (lbmx_kernels.cuh)
+    const int* special_units;      // unit offsets y*pitch + x0 handled by the general path
+    int nspecial;
+    int special_blocks;            // leading CTAs that take the special units
+    const uint32_t* special_bits;  // 1 bit per unit for special units off the perimeter, or nullptr
+    int tiles_x, tiles_y;          // interior tiles (kStageW x kStageH nodes, rows 1..ny-2)
+    int num_ctas;                  // persistent CTAs that walk the interior tiles
+    unsigned long long* tile_counter;  // next interior tile to claim (reset by the last CTA)
+    unsigned int* done_counter;        // CTAs finished in this launch
 };
 
 // perimeter index of a node on the domain edge
@@ -91,7 +102,14 @@ struct IbmArgs {
 };
 cudaError_t launch_ibm_iterate(const IbmArgs& a, cudaStream_t s);
 
-constexpr int kBlockX = 128;
-constexpr int kBlockY = 2;
+// step-kernel geometry: an interior tile is 128 x 4 nodes; each of the 256
+// consumer threads takes two x-neighbouring nodes of one row
+constexpr int kStepThreads = 288;  // 8 consumer warps + 1 producer warp
+constexpr int kConsumerWarps = 8;
+constexpr int kStageW = 128;
+constexpr int kStageH = 4;
+// guard elements before and after the population planes: staged row copies
+// reach one 16-byte chunk beyond a row segment on each side
+constexpr int kGuardElems = 64;
 
 }  // namespace lbmx

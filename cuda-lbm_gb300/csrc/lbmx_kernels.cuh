@@ -7,12 +7,25 @@
 //   [average pre-pass]      only for CM_OPT without lagged averages
 //   step kernel: pull post-stream populations (AA pattern), boundary,
 //                moments, force correction, collision, store in place.
+//
+// The step kernel works on "units" of two x-neighbouring nodes (x0 even).
+// Its first `special_blocks` CTAs take the units listed as special -- the
+// domain perimeter and every unit holding a flagged or IBM-forced node --
+// one unit per thread through the general per-node path.  The other CTAs are
+// persistent: each walks interior tiles of 128 x 4 nodes (rows 1..ny-2),
+// staged into shared memory by bulk asynchronous copies, one unit per
+// thread, and skips the special units.  An interior unit needs no boundary,
+// wrap or flag logic, reads its two nodes as one 64-bit (FP32) or 32-bit
+// (16-bit) shared-memory access wherever the pair stays aligned, collides
+// both nodes at once in packed FP32x2 arithmetic and stores in place.  The
+// AA pattern makes every population slot the property of one node, so the
+// two sets of CTAs never write the same memory.
 #pragma once
 #include "lbmx_device.cuh"
 
 namespace lbmx {
 
-constexpr int kThreads = kBlockX * kBlockY;
+constexpr int kThreads = kStepThreads;
 
 // Six FP64 sums of a block -> partials[block]; the last block to finish
 // reduces all partials in a fixed order (deterministic, unlike the
@@ -30,8 +43,8 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, double v[6], long 
         if (lane == 0) sh[warp][k] = t;
     }
     __syncthreads();
-    const unsigned nblocks = gridDim.x * gridDim.y;
-    const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+    const unsigned nblocks = gridDim.x;
+    const unsigned bid = blockIdx.x;
     if (tid == 0) {
         double t[6] = {0, 0, 0, 0, 0, 0};
         for (int w = 0; w < kThreads / 32; w++)
@@ -71,15 +84,12 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, double v[6], long 
     }
 }
 
-// Post-stream, post-boundary populations of (x, y).
+// Post-stream, post-boundary populations of (x, y); returns the node's flag.
 template <typename T>
 __device__ __forceinline__ uint8_t gather_node(const StepArgs& a, int x, int y, float f[9], unsigned* outmask) {
-    load_post_stream<T>(a, x, y, f, outmask);
-    uint8_t fl = 0;
-    if (a.flags) {
-        fl = a.flags[(long long)y * a.g.pitch + x];
-        if (fl) apply_bc(a, f, x, y, fl);
-    }
+    const uint8_t fl = a.flags ? a.flags[(long long)y * a.g.pitch + x] : (uint8_t)0;
+    load_post_stream<T>(a, x, y, fl, f, outmask);
+    if (fl) apply_bc(a, f, x, y, fl);
     return fl;
 }
 
@@ -97,96 +107,377 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
     *Fy = fy;
 }
 
+// One node through the general path (special units).
 template <typename T, int OP>
-__global__ void __launch_bounds__(kThreads) step_kernel(const StepArgs a) {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
-    double v[6] = {0, 0, 0, 0, 0, 0};
-    if (x < a.g.nx && y < a.g.ny) {
-        const long long off = (long long)y * a.g.pitch + x;
-        float f[9];
-        unsigned outmask;
-        const uint8_t fl = gather_node<T>(a, x, y, f, &outmask);
-        // macroscopics (macroscopics.cu:17-33): rho, j, raw Pi
-        float rho = 0.f, jx = 0.f, jy = 0.f;
+__device__ __forceinline__ void general_node(const StepArgs& a, int x, int y, double v[6]) {
+    const long long off = (long long)y * a.g.pitch + x;
+    float f[9];
+    unsigned outmask;
+    const uint8_t fl = gather_node<T>(a, x, y, f, &outmask);
+    // macroscopics (macroscopics.cu:17-33): rho, j, raw Pi
+    float rho = 0.f, jx = 0.f, jy = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            rho += f[q];
-            jx += (float)CX(q) * f[q];
-            jy += (float)CY(q) * f[q];
-        }
-        float Fx, Fy;
-        node_force(a, off, &Fx, &Fy);
-        // u = j/rho (macroscopics.cu:30-31), then u += F/(2 rho) (:106-107)
-        const float inv = 1.0f / rho;
-        const float ux = jx * inv + 0.5f * Fx / rho;
-        const float uy = jy * inv + 0.5f * Fy / rho;
-        float pimag = 0.f;
-        if (OP == LBMX_CM_OPT || a.partials) {
-            const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
-            const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
-            const float pxy = f[5] - f[6] + f[7] - f[8];
-            pimag = sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy);
-        }
-        if (a.rho_out) {
-            a.rho_out[off] = rho;
-            a.u_out[off] = ux;
-            a.u_out[a.g.plane + off] = uy;
-        }
-        if (a.partials) {
-            v[0] = rho;
-            v[1] = (double)rho * ux;
-            v[2] = (double)rho * uy;
-            v[3] = rho;
-            v[4] = rho * sqrtf(ux * ux + uy * uy);
-            v[5] = pimag;
-        }
-        if (a.error_word && !isfinite(rho)) atomicOr(a.error_word, 1u);
-        if (OP == LBMX_BGK) {
-            collide_bgk(f, rho, ux, uy, Fx, Fy, a.omega);
-        } else if (OP == LBMX_MRT) {
-            collide_mrt(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0);
-        } else if (OP == LBMX_CM) {
-            collide_cm(f, rho, ux, uy, Fx, Fy, a.S, -1.0f);
+    for (int q = 0; q < 9; q++) {
+        rho += f[q];
+        jx += (float)CX(q) * f[q];
+        jy += (float)CY(q) * f[q];
+    }
+    float Fx, Fy;
+    node_force(a, off, &Fx, &Fy);
+    // u = j/rho (macroscopics.cu:30-31), then u += F/(2 rho) (:106-107)
+    const float inv = 1.0f / rho;
+    const float ux = jx * inv + 0.5f * Fx / rho;
+    const float uy = jy * inv + 0.5f * Fy / rho;
+    float pimag = 0.f;
+    if (OP == LBMX_CM_OPT || a.partials) {
+        const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
+        const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
+        const float pxy = f[5] - f[6] + f[7] - f[8];
+        pimag = sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy);
+    }
+    if (a.rho_out) {
+        a.rho_out[off] = rho;
+        a.u_out[off] = ux;
+        a.u_out[a.g.plane + off] = uy;
+    }
+    if (a.partials) {
+        v[0] += rho;
+        v[1] += (double)rho * ux;
+        v[2] += (double)rho * uy;
+        v[3] += rho;
+        v[4] += rho * sqrtf(ux * ux + uy * uy);
+        v[5] += pimag;
+    }
+    if (a.check_finite && !isfinite(rho)) atomicOr(a.error_word, 1u);
+    if (OP == LBMX_BGK) {
+        collide_bgk<float>(f, rho, ux, uy, Fx, Fy, a.omega, a.forced);
+    } else if (OP == LBMX_MRT) {
+        collide_mrt<float>(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
+    } else if (OP == LBMX_CM) {
+        collide_cm<float>(f, rho, ux, uy, Fx, Fy, a.S, 0.f, false);
+    } else {
+        const float jmag = sqrtf(ux * ux + uy * uy) * rho;
+        collide_cm<float>(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate<float>(rho, jmag, pimag, a.avg), true);
+    }
+    store_post_collision<T>(a, x, y, f, outmask, fl);
+}
+
+// ---------------------------------------------------------------- staging
+// Interior tiles of kStageW x kStageH nodes are staged through a ring of
+// shared-memory buffers filled by bulk asynchronous copies
+// (cp.async.bulk, completion counted on an mbarrier), so the bytes in flight
+// per SM do not depend on how many registers the collision needs.  Each
+// (population, row) of a tile is one contiguous copy of a row segment; a
+// segment that the step reads shifted by c_x carries one extra 16-byte chunk
+// on each side, so every copy starts and ends on a 16-byte boundary.
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: gives up after `limit` polls (the caller reports the failure)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit) {
+    for (unsigned i = 0; i < limit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// orders this thread's earlier shared-memory accesses before later async-proxy writes
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+template <typename T>
+struct Staging {
+    static constexpr int A = 16 / (int)sizeof(T);   // elements per 16-byte chunk
+    static constexpr int TW = kStageW, TH = kStageH;
+    static constexpr int TWP = TW + 2 * A;           // row segment with one chunk of halo each side
+    static constexpr int NST = sizeof(T) == 4 ? 3 : 4;
+    static constexpr int STAGE_ELEMS = 9 * TH * TWP;
+    static constexpr size_t BUF_BYTES = (size_t)NST * STAGE_ELEMS * sizeof(T);
+    // after the buffers: full[NST], empty[NST] mbarriers, tile id per stage
+    static constexpr size_t SMEM = BUF_BYTES + 2 * NST * sizeof(uint64_t) + NST * sizeof(int);
+};
+
+constexpr unsigned kWaitLimit = 1u << 20;  // polls before a wait gives up
+
+// Copy of population q, tile row r: source plane, first element, element count
+// and destination column (node x sits at column x - x0 + A - shift).
+template <typename T, int P>
+__device__ __forceinline__ bool stage_copy(const StepArgs& a, int q, int r, int x0, int y0, const T** src,
+                                           unsigned* bytes, int* col) {
+    using St = Staging<T>;
+    if (y0 + r > a.g.ny - 2) return false;  // rows past the interior hold no live node
+    const int plane = q == 0 ? a.rest_plane : (P ? OPP(q) : q);
+    const int dy = P ? -CY(q) : 0;
+    const bool shifted = P && CX(q) != 0;
+    const T* F = static_cast<const T*>(a.f);
+    const long long row = (long long)(y0 + r + dy) * a.g.pitch;
+    *src = F + (long long)plane * a.g.plane + row + x0 - (shifted ? St::A : 0);
+    *bytes = (unsigned)((shifted ? St::TWP : St::TW) * sizeof(T));
+    *col = shifted ? 0 : St::A;
+    return true;
+}
+
+// Issue the copies of one tile into stage buffer `buf` (the producer warp
+// calls this; lane 0 has already armed `bar`).
+template <typename T, int P>
+__device__ __forceinline__ unsigned stage_bytes(const StepArgs& a, int tile) {
+    using St = Staging<T>;
+    const int y0 = 1 + (tile / a.tiles_x) * St::TH;
+    const int rows = min(St::TH, a.g.ny - 1 - y0);
+    // per row: P = 0 copies 9 plain segments; P = 1 copies 3 plain (c_x = 0)
+    // and 6 widened (c_x != 0) segments
+    const int per_row = P ? 3 * St::TW + 6 * St::TWP : 9 * St::TW;
+    return (unsigned)(rows * per_row * (int)sizeof(T));
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void stage_issue(const StepArgs& a, int tile, T* buf, uint64_t* bar) {
+    using St = Staging<T>;
+    const int lane = threadIdx.x & 31;
+    const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
+    const int x0 = tx * St::TW, y0 = 1 + ty * St::TH;
+    for (int c = lane; c < 9 * St::TH; c += 32) {
+        const T* src;
+        unsigned bytes;
+        int col;
+        if (stage_copy<T, P>(a, c / St::TH, c % St::TH, x0, y0, &src, &bytes, &col))
+            bulk_copy_g2s(buf + (size_t)c * St::TWP + col, src, bytes, bar);
+    }
+}
+
+// Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
+template <typename T, int OP, int P>
+__device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
+                                              double v[6]) {
+    using St = Staging<T>;
+    const Geometry& g = a.g;
+    T* F = static_cast<T*>(a.f);
+    const long long off = (long long)y * g.pitch + x0;
+    const long long plane = g.plane;
+    const int pitch = g.pitch;
+    V2 f[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        const bool shifted = P && CX(q) != 0;
+        const T* s = sbuf + (q * St::TH + r) * St::TWP + 2 * lx + (shifted ? St::A - CX(q) : St::A);
+        if (shifted) f[q].v = make_float2(Store<T>::ld(s, WQ(q)), Store<T>::ld(s + 1, WQ(q)));
+        else f[q].v = Store<T>::ld2(s, WQ(q));
+    }
+    const V2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    const V2 jx = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
+    const V2 jy = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
+    V2 Fx = {make_float2(a.body_fx, a.body_fx)}, Fy = {make_float2(a.body_fy, a.body_fy)};
+    if (a.force) {
+        Fx.v = *reinterpret_cast<const float2*>(a.force + off);
+        Fy.v = *reinterpret_cast<const float2*>(a.force + plane + off);
+    }
+    const V2 inv = vdiv(splat(1.0f, rho), rho);
+    const V2 ux = fma(0.5f * Fx, inv, jx * inv);
+    const V2 uy = fma(0.5f * Fy, inv, jy * inv);
+    V2 pimag = splat(0.f, rho);
+    if (OP == LBMX_CM_OPT || a.partials) {
+        const V2 d = (f[5] + f[6]) + (f[7] + f[8]);
+        const V2 pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
+        const V2 pxy = (f[5] + f[7]) - (f[6] + f[8]);
+        pimag = vsqrt(fma(pxx, pxx, fma(2.0f * pxy, pxy, pyy * pyy)));
+    }
+    if (a.rho_out) {
+        *reinterpret_cast<float2*>(a.rho_out + off) = rho.v;
+        *reinterpret_cast<float2*>(a.u_out + off) = ux.v;
+        *reinterpret_cast<float2*>(a.u_out + plane + off) = uy.v;
+    }
+    if (a.partials) {
+        v[0] += (double)rho.v.x + (double)rho.v.y;
+        v[1] += (double)rho.v.x * ux.v.x + (double)rho.v.y * ux.v.y;
+        v[2] += (double)rho.v.x * uy.v.x + (double)rho.v.y * uy.v.y;
+        v[3] += (double)rho.v.x + (double)rho.v.y;
+        v[4] += rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x) + rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y);
+        v[5] += (double)pimag.v.x + (double)pimag.v.y;
+    }
+    if (a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
+    if (OP == LBMX_BGK) {
+        collide_bgk<V2>(f, rho, ux, uy, Fx, Fy, a.omega, a.forced);
+    } else if (OP == LBMX_MRT) {
+        collide_mrt<V2>(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
+    } else if (OP == LBMX_CM) {
+        collide_cm<V2>(f, rho, ux, uy, Fx, Fy, a.S, rho, false);
+    } else {
+        const V2 jmag = rho * vsqrt(fma(ux, ux, uy * uy));
+        collide_cm<V2>(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate<V2>(rho, jmag, pimag, a.avg), true);
+    }
+    Store<T>::st2(F + a.rest_plane * plane + off, f[0].v, WQ(0));
+#pragma unroll
+    for (int q = 1; q < 9; q++) {
+        if (P == 0) {
+            Store<T>::st2(F + OPP(q) * plane + off, f[q].v, WQ(q));  // own slot OPP(q)
         } else {
-            const float jmag = sqrtf(ux * ux + uy * uy) * rho;
-            collide_cm(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate(rho, jmag, pimag, a.avg));
+            // slot q of the downstream nodes x + c_q
+            T* p = F + q * plane + off + (long long)CY(q) * pitch + CX(q);
+            if (CX(q) == 0) {
+                Store<T>::st2(p, f[q].v, WQ(q));
+            } else {
+                Store<T>::st(p, f[q].v.x, WQ(q));
+                Store<T>::st(p + 1, f[q].v.y, WQ(q));
+            }
         }
-        store_post_collision<T>(a, x, y, f, outmask, fl);
+    }
+}
+
+template <typename T, int OP, int P>
+__global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a) {
+    using St = Staging<T>;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    const int tid = threadIdx.x;
+    if ((int)blockIdx.x < a.special_blocks) {
+        const int u = blockIdx.x * kThreads + tid;
+        if (u < a.nspecial) {
+            const int off = a.special_units[u];
+            const int y = off / a.g.pitch, x0 = off - y * a.g.pitch;
+#pragma unroll 1
+            for (int x = x0; x < x0 + 2 && x < a.g.nx; x++) general_node<T, OP>(a, x, y, v);
+        }
+    } else {
+        // Persistent interior CTA, warp-specialised: warp 8 produces (claims
+        // the next tile from a global counter and bulk-copies it into the
+        // ring), warps 0-7 consume.  full[s] completes when a stage's bytes
+        // have landed; empty[s] when all eight consumer warps are done with it.
+        extern __shared__ __align__(128) unsigned char smem_raw[];
+        T* bufs = reinterpret_cast<T*>(smem_raw);
+        uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + St::BUF_BYTES);
+        uint64_t* empty = full + St::NST;
+        volatile int* tile_id = reinterpret_cast<volatile int*>(empty + St::NST);
+        const int ntiles = a.tiles_x * a.tiles_y;
+        const int warp = tid >> 5, lane = tid & 31;
+        if (tid == 0) {
+            for (int s = 0; s < St::NST; s++) {
+                mbar_init(&full[s], 1);
+                mbar_init(&empty[s], kConsumerWarps);
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (warp == kConsumerWarps) {
+            // producer
+            int k = 0;
+            bool failed = false;
+            for (;; k++) {
+                const int s = k % St::NST;
+                if (k >= St::NST && !mbar_wait(&empty[s], (unsigned)(((k / St::NST) - 1) & 1), kWaitLimit)) {
+                    if (lane == 0) atomicOr(a.error_word, 2u);
+                    failed = true;
+                    break;
+                }
+                int tile = 0;
+                if (lane == 0) tile = (int)atomicAdd(a.tile_counter, 1ull);
+                tile = __shfl_sync(0xffffffffu, tile, 0);
+                if (tile >= ntiles) {
+                    if (lane == 0) {
+                        tile_id[s] = -1;
+                        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&full[s])) : "memory");
+                    }
+                    break;
+                }
+                if (lane == 0) {
+                    tile_id[s] = tile;
+                    fence_proxy_async_smem();
+                    mbar_expect_tx(&full[s], stage_bytes<T, P>(a, tile));
+                }
+                __syncwarp();
+                stage_issue<T, P>(a, tile, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+            }
+            // On the normal path the consumers have waited for every fill.  If
+            // they stopped releasing stages, let the fills still unconsumed
+            // (at most one per stage) land before the CTA exits (bounded).
+            if (failed && lane == 0)
+                for (int j = max(0, k - St::NST); j < k; j++)
+                    mbar_wait(&full[j % St::NST], (unsigned)((j / St::NST) & 1), kWaitLimit);
+        } else {
+            // consumers
+            const int lx = tid % (St::TW / 2), r = tid / (St::TW / 2);
+            for (int i = 0;; i++) {
+                const int s = i % St::NST;
+                if (!mbar_wait(&full[s], (unsigned)((i / St::NST) & 1), kWaitLimit)) {
+                    if (lane == 0) atomicOr(a.error_word, 2u);
+                    break;
+                }
+                const int tile = tile_id[s];
+                if (tile < 0) break;
+                const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
+                const int x0 = tx * St::TW + 2 * lx, y = 1 + ty * St::TH + r;
+                bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
+                if (live && a.special_bits) {
+                    const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
+                    live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
+                }
+                if (live) interior_unit<T, OP, P>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&empty[s])) : "memory");
+            }
+        }
     }
     if (a.partials) block_sums(a, v, (long long)a.g.nx * a.g.ny);
+    // the last CTA to finish re-arms the tile counter for the next launch
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(a.done_counter, 1u) == gridDim.x - 1) {
+            *a.tile_counter = 0ull;
+            *a.done_counter = 0u;
+            __threadfence();
+        }
+    }
 }
 
 // Grid averages <rho>, <rho |u|>, <|Pi|> of the current step before any
 // collision (update_avg_mag, macroscopics.cuh:50-120), for CM_OPT.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a) {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
     double v[6] = {0, 0, 0, 0, 0, 0};
-    if (x < a.g.nx && y < a.g.ny) {
-        const long long off = (long long)y * a.g.pitch + x;
-        float f[9];
-        unsigned outmask;
-        gather_node<T>(a, x, y, f, &outmask);
-        float rho = 0.f, jx = 0.f, jy = 0.f;
+    const long long n = (long long)a.g.nx * a.g.ny;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
+        const int y = (int)(i / a.g.nx), xx = (int)(i - (long long)y * a.g.nx);
+        {
+            const long long off = (long long)y * a.g.pitch + xx;
+            float f[9];
+            unsigned outmask;
+            gather_node<T>(a, xx, y, f, &outmask);
+            float rho = 0.f, jx = 0.f, jy = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            rho += f[q];
-            jx += (float)CX(q) * f[q];
-            jy += (float)CY(q) * f[q];
+            for (int q = 0; q < 9; q++) {
+                rho += f[q];
+                jx += (float)CX(q) * f[q];
+                jy += (float)CY(q) * f[q];
+            }
+            float Fx, Fy;
+            node_force(a, off, &Fx, &Fy);
+            const float inv = 1.0f / rho;
+            const float ux = jx * inv + 0.5f * Fx / rho;
+            const float uy = jy * inv + 0.5f * Fy / rho;
+            const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
+            const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
+            const float pxy = f[5] - f[6] + f[7] - f[8];
+            v[3] += rho;
+            v[4] += rho * sqrtf(ux * ux + uy * uy);
+            v[5] += sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy);
         }
-        float Fx, Fy;
-        node_force(a, off, &Fx, &Fy);
-        const float inv = 1.0f / rho;
-        const float ux = jx * inv + 0.5f * Fx / rho;
-        const float uy = jy * inv + 0.5f * Fy / rho;
-        const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
-        const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
-        const float pxy = f[5] - f[6] + f[7] - f[8];
-        v[3] = rho;
-        v[4] = rho * sqrtf(ux * ux + uy * uy);
-        v[5] = sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy);
     }
     block_sums(a, v, (long long)a.g.nx * a.g.ny);
 }
@@ -216,12 +507,12 @@ __global__ void edge_prepass_kernel(const StepArgs a, float* aux) {
         else if (x == a.g.nx - 1) ix = a.g.nx - 2;
         else if (y == 0) iy = 1;
         else iy = a.g.ny - 2;
-        load_post_stream<T>(a, ix, iy, f, &m);
+        load_post_stream<T>(a, ix, iy, a.flags[(long long)iy * a.g.pitch + ix], f, &m);
 #pragma unroll
         for (int q = 0; q < 9; q++) A[q] = f[q];
     } else if (fl == LBMX_PRESSURE_OUTLET) {
         // interior node = node - 1 (pressureOutlet.cuh:12-14); x >= 1 is enforced at set_flags
-        load_post_stream<T>(a, x - 1, y, f, &m);
+        load_post_stream<T>(a, x - 1, y, a.flags[(long long)y * a.g.pitch + x - 1], f, &m);
         float r = 0.f, jx = 0.f, jy = 0.f;
 #pragma unroll
         for (int q = 0; q < 9; q++) r += f[q];
@@ -238,7 +529,7 @@ __global__ void edge_prepass_kernel(const StepArgs a, float* aux) {
         int dy = y == 0 ? y + 1 : y - 1;
         dx = max(1, min(dx, a.g.nx - 2));
         dy = max(1, min(dy, a.g.ny - 2));
-        load_post_stream<T>(a, dx, dy, f, &m);
+        load_post_stream<T>(a, dx, dy, a.flags[(long long)dy * a.g.pitch + dx], f, &m);
         float r = 0.f;
 #pragma unroll
         for (int q = 0; q < 9; q++) r += f[q];
@@ -251,8 +542,8 @@ __global__ void edge_prepass_kernel(const StepArgs a, float* aux) {
 // (init_node, src/core/init/init.cuh:12-27).
 template <typename T>
 __global__ void init_kernel(const StepArgs a, const float* rho_in, const float* u_in, int has_rest_lag) {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 4 + threadIdx.y;
     if (x >= a.g.nx || y >= a.g.ny) return;
     const long long n = (long long)a.g.nx * a.g.ny;
     const long long dn = (long long)y * a.g.nx + x;
@@ -288,20 +579,22 @@ __global__ void init_kernel(const StepArgs a, const float* rho_in, const float* 
 // Canonical post-collision populations of the last step (see lbmx.h).
 template <typename T>
 __global__ void get_populations_kernel(const StepArgs a, float* out, int last_parity) {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y * kBlockY + threadIdx.y;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 4 + threadIdx.y;
     if (x >= a.g.nx || y >= a.g.ny) return;
     const Geometry& g = a.g;
     const long long n = (long long)g.nx * g.ny;
     const long long dn = (long long)y * g.nx + x;
+    const long long row = (long long)y * g.pitch;
     const T* F = static_cast<const T*>(a.f);
-    out[dn] = Store<T>::ld(F + a.rest_plane * g.plane + (long long)y * g.pitch + x, WQ(0));
+    const uint8_t fl = a.flags ? a.flags[row + x] : (uint8_t)0;
+    out[dn] = Store<T>::ld(F + a.rest_plane * g.plane + row + x, WQ(0));
     const float nan = __int_as_float(0x7fc00000);
 #pragma unroll
     for (int q = 1; q < 9; q++) {
         float v;
         if (!last_parity) {
-            v = Store<T>::ld(F + OPP(q) * g.plane + (long long)y * g.pitch + x, WQ(q));
+            v = Store<T>::ld(F + OPP(q) * g.plane + row + x, WQ(q));
         } else {
             int dx = x + CX(q), dy = y + CY(q);
             bool out_d = false;
@@ -309,6 +602,9 @@ __global__ void get_populations_kernel(const StepArgs a, float* out, int last_pa
             if (dy < 0 || dy >= g.ny) { if (g.periodic_y) dy = dy < 0 ? dy + g.ny : dy - g.ny; else out_d = true; }
             if (!out_d) {
                 v = Store<T>::ld(F + q * g.plane + (long long)dy * g.pitch + dx, WQ(q));
+            } else if (is_halfway(fl)) {
+                // reflected into the node's own slot OPP(q), minus the wall term
+                v = Store<T>::ld(F + OPP(q) * g.plane + row + x, WQ(q)) + wall_term(a, q, fl);
             } else {
                 int sx = x - CX(q), sy = y - CY(q);
                 bool out_s = (!g.periodic_x && (sx < 0 || sx >= g.nx)) || (!g.periodic_y && (sy < 0 || sy >= g.ny));
@@ -344,25 +640,40 @@ __global__ void ibm_gather_kernel(const StepArgs a, const int* patch_nodes, int 
     pu[npatch + i] = jy * inv;
 }
 
-inline dim3 grid_of(const Geometry& g) {
-    return dim3((g.nx + kBlockX - 1) / kBlockX, (g.ny + kBlockY - 1) / kBlockY);
-}
-
-template <typename T>
-cudaError_t launch_step(const StepArgs& a, int op, cudaStream_t s) {
-    const dim3 grid = grid_of(a.g), block(kBlockX, kBlockY);
-    switch (op) {
-    case LBMX_BGK: step_kernel<T, LBMX_BGK><<<grid, block, 0, s>>>(a); break;
-    case LBMX_MRT: step_kernel<T, LBMX_MRT><<<grid, block, 0, s>>>(a); break;
-    case LBMX_CM: step_kernel<T, LBMX_CM><<<grid, block, 0, s>>>(a); break;
-    default: step_kernel<T, LBMX_CM_OPT><<<grid, block, 0, s>>>(a); break;
+template <typename T, int OP, int P>
+static cudaError_t launch_step_variant(const StepArgs& a, unsigned grid, cudaStream_t s) {
+    // the staged ring needs more than the default 48 KB; set once per device
+    static unsigned long long configured = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!(configured >> (dev & 63) & 1ull)) {
+        cudaError_t e = cudaFuncSetAttribute(step_kernel<T, OP, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Staging<T>::SMEM);
+        if (e != cudaSuccess) return e;
+        configured |= 1ull << (dev & 63);
     }
+    step_kernel<T, OP, P><<<grid, kThreads, Staging<T>::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
 template <typename T>
+cudaError_t launch_step(const StepArgs& a, int op, cudaStream_t s) {
+    const unsigned grid = (unsigned)(a.special_blocks + a.num_ctas);
+#define LBMX_STEP_CASE(OPV) \
+    return a.parity ? launch_step_variant<T, OPV, 1>(a, grid, s) : launch_step_variant<T, OPV, 0>(a, grid, s);
+    switch (op) {
+    case LBMX_BGK: LBMX_STEP_CASE(LBMX_BGK)
+    case LBMX_MRT: LBMX_STEP_CASE(LBMX_MRT)
+    case LBMX_CM: LBMX_STEP_CASE(LBMX_CM)
+    default: LBMX_STEP_CASE(LBMX_CM_OPT)
+    }
+#undef LBMX_STEP_CASE
+}
+
+template <typename T>
 cudaError_t launch_opt_prepass(const StepArgs& a, cudaStream_t s) {
-    opt_prepass_kernel<T><<<grid_of(a.g), dim3(kBlockX, kBlockY), 0, s>>>(a);
+    // as many CTAs as the step kernel, so the FP64 partials buffer fits both
+    opt_prepass_kernel<T><<<a.special_blocks + a.num_ctas, kThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -374,13 +685,15 @@ cudaError_t launch_edge_prepass(const StepArgs& a, float* aux, cudaStream_t s) {
 
 template <typename T>
 cudaError_t launch_init(const StepArgs& a, const float* rho, const float* u, cudaStream_t s) {
-    init_kernel<T><<<grid_of(a.g), dim3(kBlockX, kBlockY), 0, s>>>(a, rho, u, a.rest_plane == 9 ? 1 : 0);
+    const dim3 grid((a.g.nx + 31) / 32, (a.g.ny + 3) / 4);
+    init_kernel<T><<<grid, dim3(32, 4), 0, s>>>(a, rho, u, a.rest_plane == 9 ? 1 : 0);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_get_populations(const StepArgs& a, float* out, cudaStream_t s) {
-    get_populations_kernel<T><<<grid_of(a.g), dim3(kBlockX, kBlockY), 0, s>>>(a, out, a.parity);
+    const dim3 grid((a.g.nx + 31) / 32, (a.g.ny + 3) / 4);
+    get_populations_kernel<T><<<grid, dim3(32, 4), 0, s>>>(a, out, a.parity);
     return cudaGetLastError();
 }
 

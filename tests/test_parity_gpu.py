@@ -43,11 +43,29 @@ def compare(o, L, tol=TOL, pops=True):
         m = np.isfinite(fl)
         df = np.abs(fl[m] - fo[m]).max()
         assert df <= tol, "populations max diff %g" % df
-        if L.t % 2 == 1:  # lost slots only after a neighbour-access step
-            assert (~m).sum() < 0.1 * m.size
-        else:
-            assert m.all()
+        # the engine drops (NaN) only values that streamed out of the domain
+        assert not (~m & ~lost_slots(L, o)).any()
     return dr, du
+
+
+def lost_slots(L, o):
+    """Slots whose post-collision value left a non-periodic domain in the last step."""
+    ny, nx = L.ny, L.nx
+    lost = np.zeros((9, ny, nx), bool)
+    if L.t % 2 == 0:
+        return lost
+    per = L.params.periodic_x, L.params.periodic_y
+    cx = [0, 1, 0, -1, 0, 1, -1, -1, 1]
+    cy = [0, 0, 1, 0, -1, 1, 1, -1, -1]
+    X, Y = np.meshgrid(np.arange(nx), np.arange(ny))
+    for q in range(1, 9):
+        out = np.zeros((ny, nx), bool)
+        if not per[0]:
+            out |= (X + cx[q] < 0) | (X + cx[q] >= nx)
+        if not per[1]:
+            out |= (Y + cy[q] < 0) | (Y + cy[q] >= ny)
+        lost[q] = out
+    return lost
 
 
 @pytest.mark.parametrize("op", [C.BGK, C.MRT, C.CM])
@@ -107,9 +125,12 @@ def test_poiseuille_body_force(op, quirks):
 
 
 def test_poiseuille_cm_optimal():
+    # with the shipped regression the adapter sets the higher-order rates
+    # near 2; single-precision rounding then grows by ~x1e4 over 40 steps in
+    # the oracle's own FP32 build as well, so parity is checked on 20 steps
     c = C.poiseuille(64, 32, op=C.CM_OPT, nu=0.02, quirks=C.QUIRKS_REFERENCE)
-    o, L = run_both(c, 60)
-    compare(o, L, tol=5e-5)
+    o, L = run_both(c, 20)
+    compare(o, L, tol=1e-5)
 
 
 @pytest.mark.parametrize("quirks", [0, C.QUIRKS_REFERENCE])
@@ -161,6 +182,19 @@ def test_ragged_sizes(nx, ny):
     compare(o, L)
     c = C.random_state(C.cavity_regularized(max(nx, 4), max(ny, 4), op=C.BGK), seed=ny)
     o, L = run_both(c, 9)
+    compare(o, L)
+
+
+@pytest.mark.parametrize("case", ["cavity", "taylor_green"])
+@pytest.mark.parametrize("steps", [20, 21])
+def test_staged_tiles_many_per_cta(case, steps):
+    # 1024 x 514: 8 x 128 staged interior tiles, several per persistent CTA,
+    # so every stage of the shared-memory ring is refilled more than once
+    if case == "cavity":
+        c = C.random_state(C.cavity_moving_wall(1024, 514, op=C.MRT, nu=0.05), seed=11)
+    else:
+        c = C.random_state(C.taylor_green(1024, 514, op=C.BGK), seed=12)
+    o, L = run_both(c, steps)
     compare(o, L)
 
 
