@@ -66,6 +66,8 @@ struct lbmx_handle {
     void* f_alloc = nullptr;  // population allocation including the guard elements
     unsigned long long* tile_counter = nullptr;
     unsigned int* done_counter = nullptr;
+    int tile_chunk = 1;
+    alignas(64) CUtensorMap tmap;  // TMA descriptor of the population planes
     long long partial_cap = 0;
     char err[512] = {0};
 };
@@ -90,6 +92,38 @@ static lbmx_status fail(lbmx_handle* h, lbmx_status code, const char* fmt, ...) 
     } while (0)
 
 static size_t elem_size(int storage) { return storage == LBMX_STORAGE_F32 ? 4 : 2; }
+
+// 3-D tiled TMA descriptor over the population planes: dims {pitch, ny,
+// planes}; box {kStageW + 2 chunks of 16 bytes, kStageH, 1}; out-of-range
+// elements read as zero.  cuTensorMapEncodeTiled comes from the driver
+// through the runtime's entry-point query (no link against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static bool make_tensor_map(lbmx_handle* h, int nplanes) {
+    static EncodeTiledFn encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return false;
+        encode = reinterpret_cast<EncodeTiledFn>(fn);
+    }
+    const int es = (int)elem_size(h->p.storage);
+    const CUtensorMapDataType dt = h->p.storage == LBMX_STORAGE_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                   : h->p.storage == LBMX_STORAGE_F16_OFFSET ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                             : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    const cuuint64_t dims[3] = {(cuuint64_t)h->g.pitch, (cuuint64_t)h->g.ny, (cuuint64_t)nplanes};
+    const cuuint64_t strides[2] = {(cuuint64_t)h->g.pitch * es, (cuuint64_t)h->g.plane * es};
+    const cuuint32_t box[3] = {(cuuint32_t)(kStageW + 2 * 16 / es), (cuuint32_t)kStageH, 1u};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    return encode(&h->tmap, dt, 3, h->f, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 template <typename Fn>
 static cudaError_t dispatch(int storage, Fn fn) {
@@ -131,6 +165,7 @@ static StepArgs base_args(const lbmx_handle* h) {
     a.error_word = h->error_word;
     a.tile_counter = h->tile_counter;
     a.done_counter = h->done_counter;
+    a.tile_chunk = h->tile_chunk;
     return a;
 }
 
@@ -181,6 +216,9 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     // two persistent interior CTAs per SM walk the tiles
     const long long tiles = (long long)h->tiles_x * h->tiles_y;
     h->num_ctas = (int)std::min<long long>(tiles, 2LL * h->num_sms);
+    // claim tiles in chunks of about 1/16 of a CTA's share: few atomics on
+    // large lattices, still one tile at a time on small ones
+    h->tile_chunk = (int)std::max<long long>(1, tiles / (16LL * h->num_ctas));
     const long long blocks = h->special_blocks + h->num_ctas;
     if (blocks > h->partial_cap) {
         cudaFree(h->partials);
@@ -295,6 +333,11 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     h->f = static_cast<char*>(h->f_alloc) + (size_t)kGuardElems * elem_size(p->storage);
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (h->num_sms < 1) h->num_sms = 1;
+    if (!make_tensor_map(h, h->nplanes)) {
+        fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: cannot build the TMA descriptor (cuTensorMapEncodeTiled)");
+        lbmx_destroy(h);
+        return LBMX_ERR_CUDA;
+    }
     ALLOC(h->edge, (size_t)2 * g.perimeter * 9 * sizeof(float));
     ALLOC(h->aux, (size_t)g.perimeter * 9 * sizeof(float));
     ALLOC(h->rho_out, (size_t)g.plane * sizeof(float));
@@ -505,7 +548,7 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check) {
         a.avg_out = lagged ? h->avg : nullptr;
     }
     a.check_finite = check ? 1 : 0;
-    LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->p.op, st); }));
+    LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->tmap, h->p.op, st); }));
     h->t = s;
     return LBMX_OK;
 }

@@ -1,6 +1,7 @@
 // lbmx_internal.h -- structures shared by the host launcher and the kernels.
 #pragma once
 #include <stdint.h>
+#include <cuda.h>  // CUtensorMap (the descriptor type only; no driver calls are linked)
 #include <cuda_runtime.h>
 
 namespace lbmx {
@@ -59,6 +60,7 @@ struct StepArgs {
     int num_ctas;                  // persistent CTAs that walk the interior tiles
     unsigned long long* tile_counter;  // next interior tile to claim (reset by the last CTA)
     unsigned int* done_counter;        // CTAs finished in this launch
+    int tile_chunk;                    // consecutive tiles taken per claim
 };
 
 // perimeter index of a node on the domain edge
@@ -70,8 +72,10 @@ __host__ __device__ inline int edge_index(int x, int y, int nx, int ny) {
 }
 
 // host launchers (one translation unit per storage type)
+// tmap: 3-D tiled TMA descriptor over the population planes,
+// dims {pitch, ny, planes}, box {kStageW + 2 * 16 B of halo, kStageH, 1}
 template <typename T>
-cudaError_t launch_step(const StepArgs& a, int op, cudaStream_t s);
+cudaError_t launch_step(const StepArgs& a, const CUtensorMap& tmap, int op, cudaStream_t s);
 template <typename T>
 cudaError_t launch_edge_prepass(const StepArgs& a, float* aux, cudaStream_t s);
 template <typename T>

@@ -164,12 +164,14 @@ __device__ __forceinline__ void general_node(const StepArgs& a, int x, int y, do
 
 // ---------------------------------------------------------------- staging
 // Interior tiles of kStageW x kStageH nodes are staged through a ring of
-// shared-memory buffers filled by bulk asynchronous copies
-// (cp.async.bulk, completion counted on an mbarrier), so the bytes in flight
-// per SM do not depend on how many registers the collision needs.  Each
-// (population, row) of a tile is one contiguous copy of a row segment; a
-// segment that the step reads shifted by c_x carries one extra 16-byte chunk
-// on each side, so every copy starts and ends on a 16-byte boundary.
+// shared-memory buffers filled by the tensor memory accelerator: one 3-D
+// tiled TMA load (cp.async.bulk.tensor, completion counted on an mbarrier)
+// per population plane brings a (kStageW + halo) x kStageH box, so the bytes
+// in flight per SM do not depend on how many registers the collision needs.
+// The box starts one 16-byte chunk left of the tile and ends one chunk right
+// of it, which covers the one-node x shift of the neighbour-access step and
+// keeps the box's x coordinate on a 16-byte boundary; boxes that stick out of
+// the lattice are zero-filled by the TMA unit (those nodes are never used).
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -178,6 +180,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     uint32_t ok;
@@ -196,20 +201,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsign
 }
 // orders this thread's earlier shared-memory accesses before later async-proxy writes
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
+// 3-D tiled TMA load of one box at element coordinates (x, y, z)
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tmap, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
 }
 
 template <typename T>
 struct Staging {
     static constexpr int A = 16 / (int)sizeof(T);   // elements per 16-byte chunk
     static constexpr int TW = kStageW, TH = kStageH;
-    static constexpr int TWP = TW + 2 * A;           // row segment with one chunk of halo each side
+    static constexpr int TWP = TW + 2 * A;           // box width: the tile plus one chunk each side
     static constexpr int NST = sizeof(T) == 4 ? 3 : 4;
     static constexpr int STAGE_ELEMS = 9 * TH * TWP;
+    static constexpr unsigned STAGE_BYTES = (unsigned)(STAGE_ELEMS * sizeof(T));
     static constexpr size_t BUF_BYTES = (size_t)NST * STAGE_ELEMS * sizeof(T);
     // after the buffers: full[NST], empty[NST] mbarriers, tile id per stage
     static constexpr size_t SMEM = BUF_BYTES + 2 * NST * sizeof(uint64_t) + NST * sizeof(int);
@@ -217,50 +225,32 @@ struct Staging {
 
 constexpr unsigned kWaitLimit = 1u << 20;  // polls before a wait gives up
 
-// Copy of population q, tile row r: source plane, first element, element count
-// and destination column (node x sits at column x - x0 + A - shift).
+// Issue the nine box loads of one tile into stage buffer `buf` (producer warp;
+// lane 0 has already armed `bar` with Staging<T>::STAGE_BYTES).  Population q
+// lands at rows [q*TH, q*TH + TH); node x of tile row r then sits at column
+// x - x0 + A - (parity-1 x shift of q).
 template <typename T, int P>
-__device__ __forceinline__ bool stage_copy(const StepArgs& a, int q, int r, int x0, int y0, const T** src,
-                                           unsigned* bytes, int* col) {
-    using St = Staging<T>;
-    if (y0 + r > a.g.ny - 2) return false;  // rows past the interior hold no live node
-    const int plane = q == 0 ? a.rest_plane : (P ? OPP(q) : q);
-    const int dy = P ? -CY(q) : 0;
-    const bool shifted = P && CX(q) != 0;
-    const T* F = static_cast<const T*>(a.f);
-    const long long row = (long long)(y0 + r + dy) * a.g.pitch;
-    *src = F + (long long)plane * a.g.plane + row + x0 - (shifted ? St::A : 0);
-    *bytes = (unsigned)((shifted ? St::TWP : St::TW) * sizeof(T));
-    *col = shifted ? 0 : St::A;
-    return true;
-}
-
-// Issue the copies of one tile into stage buffer `buf` (the producer warp
-// calls this; lane 0 has already armed `bar`).
-template <typename T, int P>
-__device__ __forceinline__ unsigned stage_bytes(const StepArgs& a, int tile) {
-    using St = Staging<T>;
-    const int y0 = 1 + (tile / a.tiles_x) * St::TH;
-    const int rows = min(St::TH, a.g.ny - 1 - y0);
-    // per row: P = 0 copies 9 plain segments; P = 1 copies 3 plain (c_x = 0)
-    // and 6 widened (c_x != 0) segments
-    const int per_row = P ? 3 * St::TW + 6 * St::TWP : 9 * St::TW;
-    return (unsigned)(rows * per_row * (int)sizeof(T));
-}
-
-template <typename T, int P>
-__device__ __forceinline__ void stage_issue(const StepArgs& a, int tile, T* buf, uint64_t* bar) {
+__device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap* tmap, int tile, T* buf,
+                                            uint64_t* bar) {
     using St = Staging<T>;
     const int lane = threadIdx.x & 31;
+    if (lane >= 9) return;
+    const int q = lane;
     const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
     const int x0 = tx * St::TW, y0 = 1 + ty * St::TH;
-    for (int c = lane; c < 9 * St::TH; c += 32) {
-        const T* src;
-        unsigned bytes;
-        int col;
-        if (stage_copy<T, P>(a, c / St::TH, c % St::TH, x0, y0, &src, &bytes, &col))
-            bulk_copy_g2s(buf + (size_t)c * St::TWP + col, src, bytes, bar);
+    // parity 1 reads slot OPP(q) of the upstream nodes, rows shifted by -c_y(q)
+    int plane, dy;
+    switch (q) {
+#define LBMX_Q(QV)                                                     \
+    case QV:                                                           \
+        plane = QV == 0 ? a.rest_plane : (P ? OPP(QV) : QV);          \
+        dy = P ? -CY(QV) : 0;                                          \
+        break;
+        LBMX_Q(0) LBMX_Q(1) LBMX_Q(2) LBMX_Q(3) LBMX_Q(4) LBMX_Q(5) LBMX_Q(6) LBMX_Q(7) LBMX_Q(8)
+#undef LBMX_Q
+    default: plane = 0; dy = 0;
     }
+    tma_load_3d(buf + (size_t)q * St::TH * St::TWP, tmap, x0 - St::A, y0 + dy, plane, bar);
 }
 
 // Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
@@ -342,7 +332,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
 }
 
 template <typename T, int OP, int P>
-__global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
     using St = Staging<T>;
     double v[6] = {0, 0, 0, 0, 0, 0};
     const int tid = threadIdx.x;
@@ -375,9 +365,10 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a) {
         }
         __syncthreads();
         if (warp == kConsumerWarps) {
-            // producer
+            // producer: claims `tile_chunk` consecutive tiles per atomic
             int k = 0;
             bool failed = false;
+            int next = 0, left = 0;
             for (;; k++) {
                 const int s = k % St::NST;
                 if (k >= St::NST && !mbar_wait(&empty[s], (unsigned)(((k / St::NST) - 1) & 1), kWaitLimit)) {
@@ -385,23 +376,28 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a) {
                     failed = true;
                     break;
                 }
-                int tile = 0;
-                if (lane == 0) tile = (int)atomicAdd(a.tile_counter, 1ull);
-                tile = __shfl_sync(0xffffffffu, tile, 0);
+                if (left == 0) {
+                    int base = 0;
+                    if (lane == 0) base = (int)atomicAdd(a.tile_counter, (unsigned long long)a.tile_chunk);
+                    next = __shfl_sync(0xffffffffu, base, 0);
+                    left = a.tile_chunk;
+                }
+                const int tile = next++;
+                left--;
                 if (tile >= ntiles) {
                     if (lane == 0) {
                         tile_id[s] = -1;
-                        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&full[s])) : "memory");
+                        mbar_arrive(&full[s]);
                     }
                     break;
                 }
                 if (lane == 0) {
                     tile_id[s] = tile;
                     fence_proxy_async_smem();
-                    mbar_expect_tx(&full[s], stage_bytes<T, P>(a, tile));
+                    mbar_expect_tx(&full[s], St::STAGE_BYTES);
                 }
                 __syncwarp();
-                stage_issue<T, P>(a, tile, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+                stage_issue<T, P>(a, &tmap, tile, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
             }
             // On the normal path the consumers have waited for every fill.  If
             // they stopped releasing stages, let the fills still unconsumed
@@ -641,7 +637,7 @@ __global__ void ibm_gather_kernel(const StepArgs a, const int* patch_nodes, int 
 }
 
 template <typename T, int OP, int P>
-static cudaError_t launch_step_variant(const StepArgs& a, unsigned grid, cudaStream_t s) {
+static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tmap, unsigned grid, cudaStream_t s) {
     // the staged ring needs more than the default 48 KB; set once per device
     static unsigned long long configured = 0;
     int dev = 0;
@@ -652,15 +648,16 @@ static cudaError_t launch_step_variant(const StepArgs& a, unsigned grid, cudaStr
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    step_kernel<T, OP, P><<<grid, kThreads, Staging<T>::SMEM, s>>>(a);
+    step_kernel<T, OP, P><<<grid, kThreads, Staging<T>::SMEM, s>>>(a, tmap);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_step(const StepArgs& a, int op, cudaStream_t s) {
+cudaError_t launch_step(const StepArgs& a, const CUtensorMap& tmap, int op, cudaStream_t s) {
     const unsigned grid = (unsigned)(a.special_blocks + a.num_ctas);
-#define LBMX_STEP_CASE(OPV) \
-    return a.parity ? launch_step_variant<T, OPV, 1>(a, grid, s) : launch_step_variant<T, OPV, 0>(a, grid, s);
+#define LBMX_STEP_CASE(OPV)                                                    \
+    return a.parity ? launch_step_variant<T, OPV, 1>(a, tmap, grid, s)         \
+                    : launch_step_variant<T, OPV, 0>(a, tmap, grid, s);
     switch (op) {
     case LBMX_BGK: LBMX_STEP_CASE(LBMX_BGK)
     case LBMX_MRT: LBMX_STEP_CASE(LBMX_MRT)
@@ -706,7 +703,7 @@ cudaError_t launch_ibm_gather(const StepArgs& a, const int* patch_nodes, int npa
 }
 
 #define LBMX_INSTANTIATE(T)                                                                              \
-    template cudaError_t launch_step<T>(const StepArgs&, int, cudaStream_t);                             \
+    template cudaError_t launch_step<T>(const StepArgs&, const CUtensorMap&, int, cudaStream_t);         \
     template cudaError_t launch_opt_prepass<T>(const StepArgs&, cudaStream_t);                           \
     template cudaError_t launch_edge_prepass<T>(const StepArgs&, float*, cudaStream_t);                  \
     template cudaError_t launch_init<T>(const StepArgs&, const float*, const float*, cudaStream_t);      \
