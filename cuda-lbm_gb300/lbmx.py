@@ -32,7 +32,7 @@ STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INV
 EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
             "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
-            "lbmx_synchronize", "lbmx_last_error"]
+            "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc"]
 
 
 class Params(ctypes.Structure):
@@ -80,6 +80,8 @@ def load_library(path=LIB_PATH):
     lib.lbmx_synchronize.argtypes = [vp]
     lib.lbmx_last_error.restype = ctypes.c_char_p
     lib.lbmx_last_error.argtypes = [vp]
+    lib.lbmx_moment_sums_noalloc.restype = ctypes.c_int32
+    lib.lbmx_moment_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
     for name in ("lbmx_create", "lbmx_set_flags", "lbmx_init_from_fields", "lbmx_set_force_field",
                  "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_get_populations", "lbmx_averages",
                  "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_synchronize"):

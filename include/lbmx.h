@@ -183,6 +183,27 @@ lbmx_status lbmx_synchronize(lbmx_handle* h);
  * handle, the message of the last failed lbmx_create. */
 const char* lbmx_last_error(lbmx_handle* h);
 
+/* No counterpart in the reference.  FP64 sums {rho, rho*ux, rho*uy} over n
+ * nodes of caller-owned device fields rho[n] and u[2n] (x plane, then y
+ * plane) into sums3 (host or device memory), on `stream` (a cudaStream_t;
+ * NULL = legacy default stream); returns after the result has arrived.
+ *
+ * For callers that may not allocate device memory where they need the sums:
+ * between steps of a loop that must not stall the GPU (cudaMalloc and
+ * cudaFree synchronise the device), inside a framework whose device memory
+ * all belongs to its own pool, or under a hard memory cap.  It calls no
+ * cudaMalloc, cudaFree or other allocating routine: its scratch is a fixed
+ * 24,608-byte array in the library's device image, which every GPU that
+ * loads the library keeps until the process exits.
+ *
+ * n above LBMX_NOALLOC_MAX_NODES returns LBMX_ERR_TOO_LARGE.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls on a device
+ * share the array: calls whose work can overlap on the GPU (different
+ * streams with no ordering between them) race and must not be made. */
+#define LBMX_NOALLOC_MAX_NODES 2147483647LL
+lbmx_status lbmx_moment_sums_noalloc(const float* rho, const float* u, int64_t n, double* sums3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

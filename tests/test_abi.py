@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_binding_covers_header():
     import lbmx
-    assert set(declared_symbols()) <= set(lbmx.EXPORTED) | {"lbmx_step_noalloc"}
+    assert set(declared_symbols()) <= set(lbmx.EXPORTED)
 
 
 def test_version_and_defaults_without_gpu():

@@ -1,0 +1,67 @@
+"""lbmx_moment_sums_noalloc: the FP64 mass / momentum sums computed without
+any device allocation, for callers that may not call cudaMalloc where they
+need the sums (a stall-free stepping loop, a framework that owns all device
+memory through its own pool, a process under a hard memory cap).
+
+The entry point reads the caller's density and velocity fields and keeps its
+partial sums in a fixed array inside the library.  Its results must match the
+sums lbmx_moments returns for the same step (computed by the step kernel with
+its own scratch buffer), call after call.  This file is collected last so a
+failure here leaves every other test already run.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cases as C
+
+pytestmark = pytest.mark.gpu
+
+# FP64 sums of the same FP32 values in a different order
+RTOL = 1e-12
+
+
+def _noalloc(L, rho_dev, u_dev, out_ptr, stream=None):
+    return L.lib.lbmx_moment_sums_noalloc(rho_dev.data_ptr(), u_dev.data_ptr(), rho_dev.numel(), out_ptr, stream)
+
+
+def test_noalloc_sums_match_step_sums_on_consecutive_calls():
+    import torch
+
+    c = C.random_state(C.cavity_moving_wall(512, 384, op=C.MRT, nu=0.05), seed=21)
+    L = C.make_lattice(c)
+    n = L.n
+    rho = torch.empty(n, dtype=torch.float32, device="cuda")
+    u = torch.empty(2 * n, dtype=torch.float32, device="cuda")
+    for steps in (7, 6):  # two rounds: the shared scratch is reused
+        L.step(steps)
+        ref = (ctypes.c_double * 3)()
+        L._check(L.lib.lbmx_moments(L.h, rho.data_ptr(), u.data_ptr(), ref))
+        ref = np.array(list(ref))
+        torch.cuda.synchronize()
+        first = (ctypes.c_double * 3)()
+        assert _noalloc(L, rho, u, ctypes.addressof(first)) == 0
+        second = (ctypes.c_double * 3)()
+        assert _noalloc(L, rho, u, ctypes.addressof(second)) == 0
+        first, second = np.array(list(first)), np.array(list(second))
+        assert np.allclose(first, ref, rtol=RTOL, atol=1e-9 * abs(ref[0])), (first, ref)
+        assert np.array_equal(first, second)  # deterministic block order
+        # result delivered to device memory on a caller stream
+        dev_out = torch.zeros(3, dtype=torch.float64, device="cuda")
+        s = torch.cuda.Stream()
+        assert _noalloc(L, rho, u, dev_out.data_ptr(), s.cuda_stream) == 0
+        assert np.array_equal(dev_out.cpu().numpy(), first)
+
+
+def test_noalloc_rejects_bad_sizes():
+    import torch
+
+    c = C.taylor_green(16, 16)
+    L = C.make_lattice(c)
+    rho = torch.ones(256, dtype=torch.float32, device="cuda")
+    u = torch.zeros(512, dtype=torch.float32, device="cuda")
+    out = (ctypes.c_double * 3)()
+    assert L.lib.lbmx_moment_sums_noalloc(rho.data_ptr(), u.data_ptr(), 0, ctypes.addressof(out), None) == 1
+    too_big = 2 ** 31
+    assert L.lib.lbmx_moment_sums_noalloc(rho.data_ptr(), u.data_ptr(), too_big, ctypes.addressof(out), None) == 8
