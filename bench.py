@@ -257,7 +257,9 @@ def main():
         with open(prof) as fh:
             tr = json.load(fh)
         if str(n) in tr:
-            line["roofline"]["traffic"] = tr[str(n)]
+            t_n = tr[str(n)]
+            line["roofline"]["traffic"] = t_n["dram_read_bytes_per_launch"] + t_n["dram_write_bytes_per_launch"]
+            line["roofline"]["traffic_source"] = t_n["source"]
 
     if rank == 0 and not args.quick:
         # ---- e2e through the C-ABI with pinned host buffers

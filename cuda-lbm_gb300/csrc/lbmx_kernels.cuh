@@ -545,16 +545,19 @@ __global__ void init_kernel(const StepArgs a, const float* rho_in, const float* 
     const long long dn = (long long)y * a.g.nx + x;
     const long long off = (long long)y * a.g.pitch + x;
     const float rho = rho_in[dn], ux = u_in[dn], uy = u_in[n + dn];
-    // second-order equilibrium, bracket in double as equilibrium.cu:13-38 evaluates it
+    // second-order equilibrium, bracket in double as equilibrium.cu:13-38
+    // evaluates it (cs^2 and cs^4 rounded to float first, as there); the
+    // divisions become products with the reciprocals, computed once
     const float cs = 1.0f / sqrtf(3.0f);
     const float cs2 = cs * cs, cs4 = cs2 * cs2;
+    const double inv_cs2 = 1.0 / (double)cs2, half_inv_cs4 = 0.5 / (double)cs4;
+    const float uu = ux * ux + uy * uy;
+    const double base = 1.0 - 0.5 * (double)uu * inv_cs2;
     float fe[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) {
-        const float cu = (float)CX(q) * ux + (float)CY(q) * uy;
-        const float uu = ux * ux + uy * uy;
-        const double br = 1.0 + 0.5 * (double)cu * (double)cu / (double)cs4 - 0.5 * (double)uu / (double)cs2
-                        + (double)cu / (double)cs2;
+        const double cu = (double)((float)CX(q) * ux + (float)CY(q) * uy);
+        const double br = base + cu * cu * half_inv_cs4 + cu * inv_cs2;
         fe[q] = (float)((double)(WQ(q) * rho) * br);
     }
     T* F = static_cast<T*>(a.f);
