@@ -136,6 +136,21 @@ def time_steps(L, torch, stream, steps, warmup, flush):
     return np.array([s.elapsed_time(e) for s, e in evs])
 
 
+def max_over_ranks(value, dist, device):
+    """The slowest rank's per-step time (every rank runs its own replica)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_mlups(nodes_per_rank, ms_per_step, world):
+    """Whole-job throughput: all ranks' lattice updates over the slowest rank's time."""
+    return world * nodes_per_rank / (ms_per_step * 1e-3) / 1e6
+
+
 def l2_error(u, uref):
     return float(np.sqrt(((u - uref) ** 2).sum() / (uref ** 2).sum()))
 
@@ -230,14 +245,16 @@ def main():
 
     # ---- headline: FP32, L2 flushed before every timed step
     L = lattice(0)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
     with ClockSampler(local) as clk:
         t = time_steps(L, torch, stream, args.steps, args.warmup, flush)
-    ms = float(t.mean())
+    torch.cuda.synchronize()
     if dist is not None:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    mlups = world * nodes / (ms * 1e-3) / 1e6
+        dist.barrier()
+    ms = max_over_ranks(float(t.mean()), dist, "cuda")
+    mlups = aggregate_mlups(nodes, ms, world)
     achieved = BYTES_PER_LU[0] * nodes / (float(t.mean()) * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,

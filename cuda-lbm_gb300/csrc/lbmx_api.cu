@@ -728,6 +728,152 @@ lbmx_status lbmx_ibm_forces(lbmx_handle* h, float* force, double* drag_lift) {
 
 int64_t lbmx_time(lbmx_handle* h) { return h ? h->t : -1; }
 
+// ---------------------------------------------------------------- checkpoints
+// File: a fixed header, the population planes in the handle's storage type and
+// in-place (AA) order, the edge store, the grid averages, then a CRC-32 of
+// everything before it.  The configuration (flags, markers, forces) is the
+// caller's and is set again before a load.
+
+// CRC-32 (IEEE 802.3, reflected polynomial 0xEDB88320), table-driven
+struct Crc32Table {
+    uint32_t v[256];
+    Crc32Table() {
+        for (uint32_t i = 0; i < 256; i++) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; k++) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            v[i] = c;
+        }
+    }
+};
+
+static uint32_t crc32_update(uint32_t crc, const void* data, size_t n) {
+    static const Crc32Table table;  // thread-safe one-time construction
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    crc = ~crc;
+    for (size_t i = 0; i < n; i++) crc = table.v[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
+    return ~crc;
+}
+
+struct CheckpointHeader {
+    char magic[8];  // "LBMXCKP1"
+    int32_t nx, ny, pitch, nplanes, storage, op, periodic_x, periodic_y;
+    uint32_t quirks, reserved;
+    int64_t t;
+    int64_t f_bytes, edge_bytes;
+};
+
+lbmx_status lbmx_checkpoint_save(lbmx_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_save: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_checkpoint_save: not initialized");
+    cudaSetDevice(h->p.device);
+    CheckpointHeader hd;
+    memset(&hd, 0, sizeof(hd));
+    memcpy(hd.magic, "LBMXCKP1", 8);
+    hd.nx = h->g.nx; hd.ny = h->g.ny; hd.pitch = h->g.pitch; hd.nplanes = h->nplanes;
+    hd.storage = h->p.storage; hd.op = h->p.op; hd.periodic_x = h->g.periodic_x; hd.periodic_y = h->g.periodic_y;
+    hd.quirks = h->p.quirks; hd.t = h->t;
+    hd.f_bytes = (int64_t)h->nplanes * h->g.plane * (int64_t)elem_size(h->p.storage);
+    hd.edge_bytes = (int64_t)2 * h->g.perimeter * 9 * (int64_t)sizeof(float);
+    std::vector<char> f((size_t)hd.f_bytes), edge((size_t)hd.edge_bytes);
+    float avg[3];
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    LBMX_CUDA(h, cudaMemcpy(f.data(), h->f, f.size(), cudaMemcpyDeviceToHost));
+    LBMX_CUDA(h, cudaMemcpy(edge.data(), h->edge, edge.size(), cudaMemcpyDeviceToHost));
+    LBMX_CUDA(h, cudaMemcpy(avg, h->avg, sizeof(avg), cudaMemcpyDeviceToHost));
+    uint32_t crc = crc32_update(0, &hd, sizeof(hd));
+    crc = crc32_update(crc, f.data(), f.size());
+    crc = crc32_update(crc, edge.data(), edge.size());
+    crc = crc32_update(crc, avg, sizeof(avg));
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_save: cannot open %s", path);
+    bool ok = fwrite(&hd, sizeof(hd), 1, fp) == 1 && fwrite(f.data(), 1, f.size(), fp) == f.size() &&
+              fwrite(edge.data(), 1, edge.size(), fp) == edge.size() && fwrite(avg, sizeof(avg), 1, fp) == 1 &&
+              fwrite(&crc, sizeof(crc), 1, fp) == 1;
+    ok = (fclose(fp) == 0) && ok;
+    if (!ok) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_save: write to %s failed", path);
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_checkpoint_load(lbmx_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: NULL argument");
+    cudaSetDevice(h->p.device);
+    FILE* fp = fopen(path, "rb");
+    if (!fp) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: cannot open %s", path);
+    CheckpointHeader hd;
+    if (fread(&hd, sizeof(hd), 1, fp) != 1 || memcmp(hd.magic, "LBMXCKP1", 8) != 0) {
+        fclose(fp);
+        return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: %s is not an lbmx checkpoint", path);
+    }
+    const int64_t f_bytes = (int64_t)h->nplanes * h->g.plane * (int64_t)elem_size(h->p.storage);
+    const int64_t edge_bytes = (int64_t)2 * h->g.perimeter * 9 * (int64_t)sizeof(float);
+    if (hd.nx != h->g.nx || hd.ny != h->g.ny || hd.pitch != h->g.pitch || hd.nplanes != h->nplanes ||
+        hd.storage != h->p.storage || hd.op != h->p.op || hd.periodic_x != h->g.periodic_x ||
+        hd.periodic_y != h->g.periodic_y || hd.quirks != h->p.quirks || hd.f_bytes != f_bytes ||
+        hd.edge_bytes != edge_bytes) {
+        fclose(fp);
+        return fail(h, LBMX_ERR_INVALID_ARGUMENT,
+                    "lbmx_checkpoint_load: %s was written for a different lattice or configuration", path);
+    }
+    std::vector<char> f((size_t)f_bytes), edge((size_t)edge_bytes);
+    float avg[3];
+    uint32_t crc_file = 0;
+    const bool ok = fread(f.data(), 1, f.size(), fp) == f.size() && fread(edge.data(), 1, edge.size(), fp) == edge.size() &&
+                    fread(avg, sizeof(avg), 1, fp) == 1 && fread(&crc_file, sizeof(crc_file), 1, fp) == 1;
+    fclose(fp);
+    if (!ok) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: %s is truncated", path);
+    uint32_t crc = crc32_update(0, &hd, sizeof(hd));
+    crc = crc32_update(crc, f.data(), f.size());
+    crc = crc32_update(crc, edge.data(), edge.size());
+    crc = crc32_update(crc, avg, sizeof(avg));
+    if (crc != crc_file) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: %s fails its CRC-32", path);
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    LBMX_CUDA(h, cudaMemcpy(h->f, f.data(), f.size(), cudaMemcpyHostToDevice));
+    LBMX_CUDA(h, cudaMemcpy(h->edge, edge.data(), edge.size(), cudaMemcpyHostToDevice));
+    LBMX_CUDA(h, cudaMemcpy(h->avg, avg, sizeof(avg), cudaMemcpyHostToDevice));
+    h->t = hd.t;
+    h->initialized = true;
+    h->have_avg = h->p.op == LBMX_CM_OPT && hd.t > 0;
+    return LBMX_OK;
+}
+
+// ImageData (.vti) with appended raw Float32 density and 3-component velocity
+// (z = 0), the layout of the reference's save_vtk (src/core/lbm.cuh:269-343).
+lbmx_status lbmx_write_vti(lbmx_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_write_vti: NULL argument");
+    const Geometry& g = h->g;
+    const size_t n = (size_t)g.nx * g.ny;
+    std::vector<float> rho(n), u(2 * n);
+    lbmx_status st = lbmx_moments(h, rho.data(), u.data(), nullptr);
+    if (st != LBMX_OK) return st;
+    std::vector<float> u3(3 * n);
+    for (size_t i = 0; i < n; i++) {
+        u3[3 * i] = u[i];
+        u3[3 * i + 1] = u[n + i];
+        u3[3 * i + 2] = 0.0f;
+    }
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_write_vti: cannot open %s", path);
+    const uint64_t rho_bytes = n * sizeof(float), u_bytes = 3 * n * sizeof(float);
+    fprintf(fp, "<?xml version=\"1.0\"?>\n");
+    fprintf(fp, "<VTKFile type=\"ImageData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n");
+    fprintf(fp, "  <ImageData WholeExtent=\"0 %d 0 %d 0 0\" Origin=\"0 0 0\" Spacing=\"1 1 1\">\n", g.nx - 1, g.ny - 1);
+    fprintf(fp, "    <Piece Extent=\"0 %d 0 %d 0 0\">\n", g.nx - 1, g.ny - 1);
+    fprintf(fp, "      <PointData Scalars=\"Density\" Vectors=\"Velocity\">\n");
+    fprintf(fp, "        <DataArray type=\"Float32\" Name=\"Density\" format=\"appended\" offset=\"0\"/>\n");
+    fprintf(fp,
+            "        <DataArray type=\"Float32\" Name=\"Velocity\" NumberOfComponents=\"3\" format=\"appended\" "
+            "offset=\"%llu\"/>\n",
+            (unsigned long long)(rho_bytes + sizeof(uint64_t)));
+    fprintf(fp, "      </PointData>\n      <CellData>\n      </CellData>\n    </Piece>\n  </ImageData>\n");
+    fprintf(fp, "  <AppendedData encoding=\"raw\">\n   _");
+    bool ok = fwrite(&rho_bytes, sizeof(rho_bytes), 1, fp) == 1 && fwrite(rho.data(), 1, rho_bytes, fp) == rho_bytes &&
+              fwrite(&u_bytes, sizeof(u_bytes), 1, fp) == 1 && fwrite(u3.data(), 1, u_bytes, fp) == u_bytes;
+    fprintf(fp, "\n  </AppendedData>\n</VTKFile>\n");
+    ok = (fclose(fp) == 0) && ok;
+    if (!ok) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_write_vti: write to %s failed", path);
+    return LBMX_OK;
+}
+
 lbmx_status lbmx_synchronize(lbmx_handle* h) {
     if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_synchronize: NULL handle");
     cudaSetDevice(h->p.device);

@@ -32,7 +32,8 @@ STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INV
 EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
             "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
-            "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc"]
+            "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc", "lbmx_checkpoint_save",
+            "lbmx_checkpoint_load", "lbmx_write_vti"]
 
 
 class Params(ctypes.Structure):
@@ -80,6 +81,9 @@ def load_library(path=LIB_PATH):
     lib.lbmx_synchronize.argtypes = [vp]
     lib.lbmx_last_error.restype = ctypes.c_char_p
     lib.lbmx_last_error.argtypes = [vp]
+    for name in ("lbmx_checkpoint_save", "lbmx_checkpoint_load", "lbmx_write_vti"):
+        getattr(lib, name).restype = ctypes.c_int32
+        getattr(lib, name).argtypes = [vp, ctypes.c_char_p]
     lib.lbmx_moment_sums_noalloc.restype = ctypes.c_int32
     lib.lbmx_moment_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
     for name in ("lbmx_create", "lbmx_set_flags", "lbmx_init_from_fields", "lbmx_set_force_field",
@@ -202,6 +206,15 @@ class Lattice:
         dl = (ctypes.c_double * 2)()
         self._check(self.lib.lbmx_ibm_forces(self.h, F.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), dl))
         return F[: 2 * self.nm].reshape(2, self.nm), np.array(list(dl))
+
+    def save(self, path):
+        self._check(self.lib.lbmx_checkpoint_save(self.h, os.fsencode(path)))
+
+    def load(self, path):
+        self._check(self.lib.lbmx_checkpoint_load(self.h, os.fsencode(path)))
+
+    def write_vti(self, path):
+        self._check(self.lib.lbmx_write_vti(self.h, os.fsencode(path)))
 
     @property
     def t(self):

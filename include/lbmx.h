@@ -176,6 +176,23 @@ lbmx_status lbmx_ibm_forces(lbmx_handle* h, float* force, double* drag_lift);
 /* Steps taken since lbmx_init_from_fields. */
 int64_t lbmx_time(lbmx_handle* h);
 
+/* No counterpart in the reference (it writes output only, never state).
+ * Save the dynamic state -- populations in storage form, the edge store, the
+ * step count and the CM_OPT averages -- with a CRC-32; loading it into a
+ * handle created with the same params (and given the same flags, force and
+ * markers) continues bit for bit.  A file for another lattice, storage,
+ * operator or quirk set, or one that fails its CRC, is rejected with
+ * LBMX_ERR_INVALID_ARGUMENT. */
+lbmx_status lbmx_checkpoint_save(lbmx_handle* h, const char* path);
+lbmx_status lbmx_checkpoint_load(lbmx_handle* h, const char* path);
+
+/* Replaces LBM::save_vtk (src/core/lbm.cuh:269-343): ImageData .vti with
+ * appended raw Float32 density and 3-component velocity (z = 0) of the last
+ * stored step.  The velocity array's offset counts the 8-byte length header
+ * of the density array, as the VTK appended format defines it (the
+ * reference's offset omits it). */
+lbmx_status lbmx_write_vti(lbmx_handle* h, const char* path);
+
 /* Waits for the handle's stream. */
 lbmx_status lbmx_synchronize(lbmx_handle* h);
 

@@ -1,0 +1,73 @@
+"""Checkpoint / restart and .vti output through the C-ABI.
+
+A checkpoint holds the dynamic state only (populations in storage form, the
+edge store, the step count, the CM_OPT averages) plus a CRC-32; a handle
+built with the same params, flags, force and markers continues bit for bit.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases as C
+import lbmx
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("storage", [0, 1])
+@pytest.mark.parametrize("k", [3, 4])
+def test_restart_is_bit_exact(tmp_path, storage, k):
+    c = C.random_state(C.cavity_regularized(96, 64, op=C.MRT, quirks=C.QUIRKS_REFERENCE), seed=5)
+    a = C.make_lattice(c, storage=storage)
+    a.step(k)
+    a.save(str(tmp_path / "s.ckpt"))
+    a.step(11)
+    ra, ua, _ = a.moments()
+    b = C.make_lattice(c, storage=storage)
+    b.load(str(tmp_path / "s.ckpt"))
+    assert b.t == k
+    b.step(11)
+    rb, ub, _ = b.moments()
+    assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
+    assert np.array_equal(np.nan_to_num(a.populations()), np.nan_to_num(b.populations()))
+
+
+def test_restart_rejects_corrupt_or_foreign_files(tmp_path):
+    c = C.taylor_green(64, 48, op=C.BGK)
+    a = C.make_lattice(c)
+    a.step(2)
+    path = str(tmp_path / "s.ckpt")
+    a.save(path)
+    raw = bytearray(open(path, "rb").read())
+    raw[200] ^= 0x40
+    bad = str(tmp_path / "bad.ckpt")
+    open(bad, "wb").write(raw)
+    with pytest.raises(lbmx.LbmxError) as e:
+        C.make_lattice(c).load(bad)
+    assert "CRC" in str(e.value)
+    other = C.make_lattice(C.taylor_green(64, 32, op=C.BGK))
+    with pytest.raises(lbmx.LbmxError):
+        other.load(path)
+    with pytest.raises(lbmx.LbmxError):
+        C.make_lattice(c, storage=1).load(path)
+
+
+def test_vti_holds_the_stored_moments(tmp_path):
+    c = C.random_state(C.taylor_green(40, 24, op=C.MRT), seed=2)
+    L = C.make_lattice(c)
+    L.step(5)
+    rho, u, _ = L.moments()
+    path = str(tmp_path / "out.vti")
+    L.write_vti(path)
+    data = open(path, "rb").read()
+    head, _, rest = data.partition(b"<AppendedData encoding=\"raw\">\n   _")
+    assert b'WholeExtent="0 39 0 23 0 0"' in head
+    n = 40 * 24
+    nb = int(np.frombuffer(rest[:8], np.uint64)[0])
+    assert nb == 4 * n
+    r = np.frombuffer(rest[8:8 + nb], np.float32).reshape(24, 40)
+    nv = int(np.frombuffer(rest[8 + nb:16 + nb], np.uint64)[0])
+    v = np.frombuffer(rest[16 + nb:16 + nb + nv], np.float32).reshape(24, 40, 3)
+    assert np.array_equal(r, rho)
+    assert np.array_equal(v[..., 0], u[0]) and np.array_equal(v[..., 1], u[1]) and not v[..., 2].any()
