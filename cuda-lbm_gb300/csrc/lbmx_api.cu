@@ -12,65 +12,13 @@
 #include <algorithm>
 #include <vector>
 
-#include "lbmx.h"
-#include "lbmx_internal.h"
+#include "lbmx_handle.h"
 
 namespace lbmx {
 size_t ibm_smem_bytes(int npatch, int nm);
 }
 
 using namespace lbmx;
-
-struct lbmx_handle {
-    lbmx_params p;
-    Geometry g;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    void* f = nullptr;
-    int nplanes = 9;
-    uint8_t* flags = nullptr;      // device, pitched; null while every node is fluid
-    bool has_aux_bc = false;
-    float* edge = nullptr;         // [2][perimeter][9]
-    float* aux = nullptr;          // [perimeter][9]
-    float* force = nullptr;        // [2][plane] optional per-node body force
-    float* ibm_force = nullptr;    // [2][plane]
-    float* rho_out = nullptr;      // [plane]
-    float* u_out = nullptr;        // [2][plane]
-    float* staging = nullptr;      // dense [3][n] upload / readback staging
-    float* pop_out = nullptr;      // dense [9][n] readback staging
-    double* partials = nullptr;    // [blocks][6]
-    unsigned int* counter = nullptr;
-    double* sums = nullptr;        // [6]
-    float* avg = nullptr;          // [3]
-    unsigned int* error_word = nullptr;
-    long long blocks = 0;
-    long long t = 0;
-    bool initialized = false;
-    bool have_avg = false;
-    // immersed boundary
-    int nm = 0, npatch = 0, stencil = 0;
-    int* patch_nodes = nullptr;
-    int* sten_idx = nullptr;
-    float* sten_w = nullptr;
-    float* patch_rho = nullptr;
-    float* patch_u = nullptr;
-    float* marker_u = nullptr;
-    float* marker_rho = nullptr;
-    float* marker_force = nullptr;
-    std::vector<int> patch_host;   // IBM patch node offsets
-    // work split of the step kernel
-    std::vector<uint8_t> flags_host;  // pitched copy of the flags (empty: all fluid)
-    int* special_units = nullptr;
-    uint32_t* special_bits = nullptr;
-    int nspecial = 0, special_blocks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
-    void* f_alloc = nullptr;  // population allocation including the guard elements
-    unsigned long long* tile_counter = nullptr;
-    unsigned int* done_counter = nullptr;
-    int tile_chunk = 1;
-    alignas(64) CUtensorMap tmap;  // TMA descriptor of the population planes
-    long long partial_cap = 0;
-    char err[512] = {0};
-};
 
 static char g_create_err[512];
 
@@ -91,17 +39,17 @@ static lbmx_status fail(lbmx_handle* h, lbmx_status code, const char* fmt, ...) 
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);        \
     } while (0)
 
-static size_t elem_size(int storage) { return storage == LBMX_STORAGE_F32 ? 4 : 2; }
+size_t lbmx::elem_size(int storage) { return storage == LBMX_STORAGE_F32 ? 4 : 2; }
 
 // 3-D tiled TMA descriptor over the population planes: dims {pitch, ny,
-// planes}; box {kStageW + 2 chunks of 16 bytes, kStageH, 1}; out-of-range
+// planes}; box {tile_w + 2 chunks of 16 bytes, tile_h, 1}; out-of-range
 // elements read as zero.  cuTensorMapEncodeTiled comes from the driver
 // through the runtime's entry-point query (no link against libcuda).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-static bool make_tensor_map(lbmx_handle* h, int nplanes) {
+bool lbmx::encode_population_map(const lbmx_handle* h, CUtensorMap* out, int tile_w, int tile_h) {
     static EncodeTiledFn encode = nullptr;
     if (!encode) {
         void* fn = nullptr;
@@ -116,25 +64,16 @@ static bool make_tensor_map(lbmx_handle* h, int nplanes) {
     const CUtensorMapDataType dt = h->p.storage == LBMX_STORAGE_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                    : h->p.storage == LBMX_STORAGE_F16_OFFSET ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                                              : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-    const cuuint64_t dims[3] = {(cuuint64_t)h->g.pitch, (cuuint64_t)h->g.ny, (cuuint64_t)nplanes};
+    const cuuint64_t dims[3] = {(cuuint64_t)h->g.pitch, (cuuint64_t)h->g.ny, (cuuint64_t)h->nplanes};
     const cuuint64_t strides[2] = {(cuuint64_t)h->g.pitch * es, (cuuint64_t)h->g.plane * es};
-    const cuuint32_t box[3] = {(cuuint32_t)(kStageW + 2 * 16 / es), (cuuint32_t)kStageH, 1u};
+    const cuuint32_t box[3] = {(cuuint32_t)(tile_w + 2 * 16 / es), (cuuint32_t)tile_h, 1u};
     const cuuint32_t estr[3] = {1u, 1u, 1u};
-    return encode(&h->tmap, dt, 3, h->f, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    return encode(out, dt, 3, h->f, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <typename Fn>
-static cudaError_t dispatch(int storage, Fn fn) {
-    switch (storage) {
-    case LBMX_STORAGE_F16_OFFSET: return fn(__half());
-    case LBMX_STORAGE_BF16_OFFSET: return fn(__nv_bfloat16());
-    default: return fn(float());
-    }
-}
-
-static StepArgs base_args(const lbmx_handle* h) {
+StepArgs lbmx::base_args(const lbmx_handle* h) {
     StepArgs a;
     memset(&a, 0, sizeof(a));
     a.g = h->g;
@@ -243,7 +182,7 @@ static lbmx_status check_pipeline(lbmx_handle* h) {
 }
 
 // parity and rest-population plane of step index s (1-based)
-static void set_step(const lbmx_handle* h, StepArgs& a, long long s) {
+void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.parity = (int)(s & 1);
     a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? (a.parity ? 9 : 0) : 0;
 }
@@ -333,7 +272,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     h->f = static_cast<char*>(h->f_alloc) + (size_t)kGuardElems * elem_size(p->storage);
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (h->num_sms < 1) h->num_sms = 1;
-    if (!make_tensor_map(h, h->nplanes)) {
+    if (!encode_population_map(h, &h->tmap, kStageW, kStageH)) {
         fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: cannot build the TMA descriptor (cuTensorMapEncodeTiled)");
         lbmx_destroy(h);
         return LBMX_ERR_CUDA;

@@ -1,0 +1,82 @@
+// lbmx_handle.h -- the state behind an lbmx_handle, shared by the C-ABI
+// translation units (lbmx_api.cu, lbmx_batch.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <vector>
+
+#include "lbmx.h"
+#include "lbmx_internal.h"
+
+struct lbmx_handle {
+    lbmx_params p;
+    lbmx::Geometry g;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void* f = nullptr;
+    int nplanes = 9;
+    uint8_t* flags = nullptr;      // device, pitched; null while every node is fluid
+    bool has_aux_bc = false;
+    float* edge = nullptr;         // [2][perimeter][9]
+    float* aux = nullptr;          // [perimeter][9]
+    float* force = nullptr;        // [2][plane] optional per-node body force
+    float* ibm_force = nullptr;    // [2][plane]
+    float* rho_out = nullptr;      // [plane]
+    float* u_out = nullptr;        // [2][plane]
+    float* staging = nullptr;      // dense [3][n] upload / readback staging
+    float* pop_out = nullptr;      // dense [9][n] readback staging
+    double* partials = nullptr;    // [blocks][6]
+    unsigned int* counter = nullptr;
+    double* sums = nullptr;        // [6]
+    float* avg = nullptr;          // [3]
+    unsigned int* error_word = nullptr;
+    long long blocks = 0;
+    long long t = 0;
+    bool initialized = false;
+    bool have_avg = false;
+    // immersed boundary
+    int nm = 0, npatch = 0, stencil = 0;
+    int* patch_nodes = nullptr;
+    int* sten_idx = nullptr;
+    float* sten_w = nullptr;
+    float* patch_rho = nullptr;
+    float* patch_u = nullptr;
+    float* marker_u = nullptr;
+    float* marker_rho = nullptr;
+    float* marker_force = nullptr;
+    std::vector<int> patch_host;   // IBM patch node offsets
+    // work split of the step kernel
+    std::vector<uint8_t> flags_host;  // pitched copy of the flags (empty: all fluid)
+    int* special_units = nullptr;
+    uint32_t* special_bits = nullptr;
+    int nspecial = 0, special_blocks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
+    void* f_alloc = nullptr;  // population allocation including the guard elements
+    unsigned long long* tile_counter = nullptr;
+    unsigned int* done_counter = nullptr;
+    int tile_chunk = 1;
+    alignas(64) CUtensorMap tmap;  // TMA descriptor of the population planes
+    long long partial_cap = 0;
+    char err[512] = {0};
+};
+
+namespace lbmx {
+
+size_t elem_size(int storage);
+// kernel arguments of the handle's current configuration (no step yet)
+StepArgs base_args(const lbmx_handle* h);
+// parity and rest-population plane of step index s (1-based)
+void set_step(const lbmx_handle* h, StepArgs& a, long long s);
+// 3-D tiled TMA descriptor over the population planes for tile_w x tile_h tiles
+bool encode_population_map(const lbmx_handle* h, CUtensorMap* out, int tile_w, int tile_h);
+
+template <typename Fn>
+cudaError_t dispatch(int storage, Fn fn) {
+    switch (storage) {
+    case LBMX_STORAGE_F16_OFFSET: return fn(__half());
+    case LBMX_STORAGE_BF16_OFFSET: return fn(__nv_bfloat16());
+    default: return fn(float());
+    }
+}
+
+}  // namespace lbmx

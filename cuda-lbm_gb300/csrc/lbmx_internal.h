@@ -106,12 +106,33 @@ struct IbmArgs {
 };
 cudaError_t launch_ibm_iterate(const IbmArgs& a, cudaStream_t s);
 
+// Many lattices in one persistent launch (lbmx_batch.cu).  Work items are
+// interior tiles and chunks of special units of every lattice; the
+// persistent CTAs claim them from one counter in list order.
+struct BatchArgs {
+    const StepArgs* lat;          // [count] per-lattice arguments of this launch
+    const CUtensorMap* tmaps;     // [count] TMA descriptors for the launch's tile width (64-byte aligned)
+    const int2* items;            // {lattice, tile >= 0 | -(special chunk + 1)}
+    int nitems;
+    int chunk;                    // items claimed per atomic
+    unsigned long long* counter;  // next item (reset by the last CTA)
+    unsigned int* done;           // CTAs finished in this launch
+    unsigned int* error_word;     // bit 1: a staging wait gave up
+};
+// tile shape tile_w x tile_h: 64 x 8, 128 x 4 or 128 x 8; op: BGK, MRT or CM;
+// grid 0 only prepares the kernel (attributes) for a later graph capture
+template <typename T>
+cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w, int tile_h, unsigned grid,
+                              cudaStream_t s);
+
 // step-kernel geometry: an interior tile is 128 x 4 nodes; each of the 256
-// consumer threads takes two x-neighbouring nodes of one row
+// consumer threads takes two x-neighbouring nodes of one row.  The batched
+// kernel also runs 64 x 8 and 128 x 8 tiles.
 constexpr int kStepThreads = 288;  // 8 consumer warps + 1 producer warp
 constexpr int kConsumerWarps = 8;
 constexpr int kStageW = 128;
 constexpr int kStageH = 4;
+constexpr int kSpecialChunk = kConsumerWarps * 32;  // special units per batched work item
 // guard elements before and after the population planes: staged row copies
 // reach one 16-byte chunk beyond a row segment on each side
 constexpr int kGuardElems = 64;

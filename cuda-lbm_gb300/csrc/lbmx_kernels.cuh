@@ -107,9 +107,12 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
     *Fy = fy;
 }
 
-// One node through the general path (special units).
+// One node through the general path (special units).  Kept out of line: the
+// single-lattice and the batched step kernels then run the same compiled
+// code for boundary nodes, so a lattice gets bit-identical results from both
+// (inlined, the two callers may contract multiply-adds differently).
 template <typename T, int OP>
-__device__ __forceinline__ void general_node(const StepArgs& a, int x, int y, double v[6]) {
+__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, double v[6]) {
     const long long off = (long long)y * a.g.pitch + x;
     float f[9];
     unsigned outmask;
@@ -210,14 +213,19 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tmap, 
         : "memory");
 }
 
-template <typename T>
+template <typename T, int TW_ = kStageW, int TH_ = kStageH>
 struct Staging {
     static constexpr int A = 16 / (int)sizeof(T);   // elements per 16-byte chunk
-    static constexpr int TW = kStageW, TH = kStageH;
+    static constexpr int TW = TW_, TH = TH_;
+    static constexpr int ROWS = 2 * kConsumerWarps * 32 / TW;  // tile rows one pass of the consumers covers
     static constexpr int TWP = TW + 2 * A;           // box width: the tile plus one chunk each side
     static constexpr int NST = sizeof(T) == 4 ? 3 : 4;
-    static constexpr int STAGE_ELEMS = 9 * TH * TWP;
-    static constexpr unsigned STAGE_BYTES = (unsigned)(STAGE_ELEMS * sizeof(T));
+    // one population's box, its slot padded to 128 bytes: every box lands on
+    // a 128-byte boundary of shared memory
+    static constexpr int BOX_ELEMS = TH * TWP;
+    static constexpr int SLAB = (int)(((BOX_ELEMS * sizeof(T) + 127) / 128) * 128 / sizeof(T));
+    static constexpr int STAGE_ELEMS = 9 * SLAB;
+    static constexpr unsigned STAGE_BYTES = (unsigned)(9 * BOX_ELEMS * sizeof(T));  // bytes the nine boxes bring
     static constexpr size_t BUF_BYTES = (size_t)NST * STAGE_ELEMS * sizeof(T);
     // after the buffers: full[NST], empty[NST] mbarriers, tile id per stage
     static constexpr size_t SMEM = BUF_BYTES + 2 * NST * sizeof(uint64_t) + NST * sizeof(int);
@@ -227,12 +235,12 @@ constexpr unsigned kWaitLimit = 1u << 20;  // polls before a wait gives up
 
 // Issue the nine box loads of one tile into stage buffer `buf` (producer warp;
 // lane 0 has already armed `bar` with Staging<T>::STAGE_BYTES).  Population q
-// lands at rows [q*TH, q*TH + TH); node x of tile row r then sits at column
-// x - x0 + A - (parity-1 x shift of q).
-template <typename T, int P>
+// lands in slab q (TH rows of TWP elements); node x of tile row r then sits at
+// column x - x0 + A - (parity-1 x shift of q).
+template <typename T, int P, int TW = kStageW, int TH = kStageH>
 __device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap* tmap, int tile, T* buf,
                                             uint64_t* bar) {
-    using St = Staging<T>;
+    using St = Staging<T, TW, TH>;
     const int lane = threadIdx.x & 31;
     if (lane >= 9) return;
     const int q = lane;
@@ -250,14 +258,14 @@ __device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap
 #undef LBMX_Q
     default: plane = 0; dy = 0;
     }
-    tma_load_3d(buf + (size_t)q * St::TH * St::TWP, tmap, x0 - St::A, y0 + dy, plane, bar);
+    tma_load_3d(buf + (size_t)q * St::SLAB, tmap, x0 - St::A, y0 + dy, plane, bar);
 }
 
 // Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
-template <typename T, int OP, int P>
+template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
                                               double v[6]) {
-    using St = Staging<T>;
+    using St = Staging<T, TW, TH>;
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
     const long long off = (long long)y * g.pitch + x0;
@@ -267,7 +275,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
 #pragma unroll
     for (int q = 0; q < 9; q++) {
         const bool shifted = P && CX(q) != 0;
-        const T* s = sbuf + (q * St::TH + r) * St::TWP + 2 * lx + (shifted ? St::A - CX(q) : St::A);
+        const T* s = sbuf + q * St::SLAB + r * St::TWP + 2 * lx + (shifted ? St::A - CX(q) : St::A);
         if (shifted) f[q].v = make_float2(Store<T>::ld(s, WQ(q)), Store<T>::ld(s + 1, WQ(q)));
         else f[q].v = Store<T>::ld2(s, WQ(q));
     }

@@ -33,7 +33,9 @@ EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy"
             "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
             "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc", "lbmx_checkpoint_save",
-            "lbmx_checkpoint_load", "lbmx_write_vti"]
+            "lbmx_checkpoint_load", "lbmx_write_vti", "lbmx_batch_create", "lbmx_batch_destroy",
+            "lbmx_batch_set_config", "lbmx_batch_get_config", "lbmx_batch_autotune", "lbmx_batch_step",
+            "lbmx_batch_synchronize", "lbmx_batch_last_error"]
 
 
 class Params(ctypes.Structure):
@@ -49,6 +51,15 @@ class Params(ctypes.Structure):
         ("body_fx", ctypes.c_float), ("body_fy", ctypes.c_float),
         ("stream", ctypes.c_void_p),
     ]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("tile_w", ctypes.c_int32), ("tile_h", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("chunk", ctypes.c_int32),
+                ("graph_steps", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class LbmxError(RuntimeError):
@@ -84,6 +95,18 @@ def load_library(path=LIB_PATH):
     for name in ("lbmx_checkpoint_save", "lbmx_checkpoint_load", "lbmx_write_vti"):
         getattr(lib, name).restype = ctypes.c_int32
         getattr(lib, name).argtypes = [vp, ctypes.c_char_p]
+    lib.lbmx_batch_create.argtypes = [P(vp), ctypes.c_int32, P(vp)]
+    lib.lbmx_batch_destroy.argtypes = [vp]
+    lib.lbmx_batch_set_config.argtypes = [vp, P(BatchConfig)]
+    lib.lbmx_batch_get_config.argtypes = [vp, P(BatchConfig)]
+    lib.lbmx_batch_autotune.argtypes = [vp, ctypes.c_int32, P(BatchConfig)]
+    lib.lbmx_batch_step.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32]
+    lib.lbmx_batch_synchronize.argtypes = [vp]
+    lib.lbmx_batch_last_error.restype = ctypes.c_char_p
+    lib.lbmx_batch_last_error.argtypes = [vp]
+    for name in ("lbmx_batch_create", "lbmx_batch_set_config", "lbmx_batch_get_config", "lbmx_batch_autotune",
+                 "lbmx_batch_step", "lbmx_batch_synchronize"):
+        getattr(lib, name).restype = ctypes.c_int32
     lib.lbmx_moment_sums_noalloc.restype = ctypes.c_int32
     lib.lbmx_moment_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
     for name in ("lbmx_create", "lbmx_set_flags", "lbmx_init_from_fields", "lbmx_set_force_field",
@@ -222,3 +245,53 @@ class Lattice:
 
     def synchronize(self):
         self._check(self.lib.lbmx_synchronize(self.h))
+
+
+class Batch:
+    """Many lattices advanced by one persistent launch per step (lbmx_batch_*).
+
+    The lattices stay ordinary Lattice objects (read them as usual); they
+    must outlive the batch."""
+
+    def __init__(self, lattices):
+        self.lib = lib()
+        self.lattices = list(lattices)
+        arr = (ctypes.c_void_p * len(self.lattices))(*[L.h.value for L in self.lattices])
+        b = ctypes.c_void_p()
+        rc = self.lib.lbmx_batch_create(arr, len(self.lattices), ctypes.byref(b))
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_batch_last_error(None).decode())
+        self.b = b
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_batch_last_error(self.b).decode())
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.lbmx_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def config(self):
+        c = BatchConfig()
+        self._check(self.lib.lbmx_batch_get_config(self.b, ctypes.byref(c)))
+        return c.as_dict()
+
+    def set_config(self, tile_w=128, tile_h=4, ctas_per_sm=2, chunk=1, graph_steps=16):
+        c = BatchConfig(tile_w, tile_h, ctas_per_sm, chunk, graph_steps)
+        self._check(self.lib.lbmx_batch_set_config(self.b, ctypes.byref(c)))
+
+    def autotune(self, trial_steps=8):
+        c = BatchConfig()
+        self._check(self.lib.lbmx_batch_autotune(self.b, int(trial_steps), ctypes.byref(c)))
+        return c.as_dict()
+
+    def step(self, n=1, flags=STEP_STORE_MOMENTS):
+        self._check(self.lib.lbmx_batch_step(self.b, int(n), int(flags)))
+
+    def synchronize(self):
+        self._check(self.lib.lbmx_batch_synchronize(self.b))

@@ -221,6 +221,45 @@ const char* lbmx_last_error(lbmx_handle* h);
 #define LBMX_NOALLOC_MAX_NODES 2147483647LL
 lbmx_status lbmx_moment_sums_noalloc(const float* rho, const float* u, int64_t n, double* sums3, void* stream);
 
+/* ------------------------------------------------------------------ batches
+ * No counterpart in the reference, which runs one lattice per process
+ * (src/main.cu:96-114).  A batch advances many independent lattices -- any
+ * sizes, relaxation rates, flags and forces -- in one persistent kernel
+ * launch per step, replayed from CUDA graphs.  Every step gives each lattice
+ * bit for bit what lbmx_step gives it alone.
+ *
+ * The lattices are ordinary handles, created, flagged and initialised as
+ * usual and still read with lbmx_moments / lbmx_get_populations /
+ * lbmx_checkpoint_save.  They must share device, storage and operator (BGK,
+ * MRT or CM; not CM_OPT), carry no IBM markers and stand at the same step
+ * count; each lattice's stream waits for the batch's steps.  Batched steps
+ * leave the FP64 sums of lbmx_moments untouched.  Destroy the batch before
+ * its lattices. */
+typedef struct lbmx_batch lbmx_batch;
+
+typedef struct lbmx_batch_config {
+    int32_t tile_w;       /* interior tile shape tile_w x tile_h: 64 x 8, 128 x 4 or 128 x 8 */
+    int32_t tile_h;
+    int32_t ctas_per_sm;  /* persistent CTAs per SM: 1 or 2 */
+    int32_t chunk;        /* work items claimed per atomic: 1..64 */
+    int32_t graph_steps;  /* steps per CUDA graph replay: 0 (no graph) or even, <= 64 */
+} lbmx_batch_config;
+
+lbmx_status lbmx_batch_create(lbmx_handle* const* lattices, int32_t count, lbmx_batch** out);
+void lbmx_batch_destroy(lbmx_batch* b);
+lbmx_status lbmx_batch_set_config(lbmx_batch* b, const lbmx_batch_config* cfg);
+lbmx_status lbmx_batch_get_config(lbmx_batch* b, lbmx_batch_config* cfg);
+/* Time every configuration for trial_steps steps (after two warm-up steps)
+ * and keep the fastest; the lattices are put back as they were. */
+lbmx_status lbmx_batch_autotune(lbmx_batch* b, int32_t trial_steps, lbmx_batch_config* chosen);
+/* nsteps steps of every lattice; flags as lbmx_step_ex (a non-finite
+ * density in any lattice gives LBMX_ERR_NONFINITE). */
+lbmx_status lbmx_batch_step(lbmx_batch* b, int32_t nsteps, uint32_t flags);
+lbmx_status lbmx_batch_synchronize(lbmx_batch* b);
+/* Message of the last failed call on this batch; with NULL, of the last
+ * failed lbmx_batch_create. */
+const char* lbmx_batch_last_error(lbmx_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

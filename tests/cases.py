@@ -146,3 +146,18 @@ def make_lattice(c, storage=0, options=0):
     if c["markers"] is not None:
         L.set_markers(c["markers"])
     return L
+
+
+def ensemble(count=512, seed=0, sides=tuple(range(64, 769, 32)), re_range=(100.0, 5000.0), u_lid=0.1):
+    """The batched-ensemble workload: `count` lid-driven cavities, side lengths
+    drawn uniformly from {64, 96, ..., 768} and Reynolds numbers log-uniform in
+    [100, 5000] (numpy PCG64, seed 0); nu = u_lid * side / Re."""
+    rng = np.random.default_rng(seed)
+    s = rng.choice(np.asarray(sides), size=count)
+    re = np.exp(rng.uniform(np.log(re_range[0]), np.log(re_range[1]), size=count))
+    return [(int(a), float(b), u_lid * float(a) / float(b)) for a, b in zip(s, re)]
+
+
+def ensemble_cavity(side, nu, op=MRT, u_lid=0.1):
+    """One cavity of the ensemble: rho = 1, u = 0, half-way walls, moving lid."""
+    return cavity_moving_wall(side, side, op=op, nu=nu, u_lid=u_lid)
