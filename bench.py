@@ -6,9 +6,9 @@ half-way moving wall, half-way bounce-back on the other walls, Re = 1000
 (nu = u L / Re with L = NY, src/main.cu:66), rho = 1 and u = 0 initially.
 
   value     MLUPS of the fused step kernel, FP32 storage, inputs resident in
-            HBM; every timed step is preceded by a 256 MB write that flushes
-            L2 (the 1024^2 lattice, 38 MB per population set, would
-            otherwise stay in the 129 MB L2).
+            HBM; every timed step is preceded by an L2 flush (a 256 MB write,
+            then a 256 MB read of a second buffer) -- the 1024^2 lattice,
+            38 MB per population set, would otherwise stay in the 129 MB L2.
   e2e       the same metric through the C-ABI with host buffers: fields
             uploaded from pinned host memory, lbmx_step once per LBM step
             with the FP64 mass/momentum sums read back every step (the
@@ -19,6 +19,11 @@ half-way moving wall, half-way bounce-back on the other walls, Re = 1000
             steps.
   hbm_bound the same kernel on an 8192 x 8192 cavity (2.4 GB per population
             set, far above L2) for the roofline fraction without a flush.
+  ensemble  the batched-ensemble workload: 512 lid-driven cavities of
+            uneven sizes and Reynolds numbers in one persistent launch per
+            step (CUDA graphs, autotuned tile shape), aggregate MLUPS for
+            FP16-offset and FP32 storage and the per-instance L2 velocity
+            error of the smallest instances against the FP64 oracle.
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on the same
             workload, 200 steps.
 
@@ -117,18 +122,34 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class L2Flush:
+    """Evicts the lattice from L2 between timed steps: a 256 MB write (twice
+    the 129 MB L2), then a 256 MB read of a second buffer, so L2 holds only
+    clean, unrelated lines when the step starts (the step then pays neither
+    for its own data being cached nor for writing back the flush's)."""
+
+    def __init__(self, torch):
+        self.w = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+        self.r = torch.ones(64 << 20, dtype=torch.float32, device="cuda")
+        self.acc = torch.zeros(1, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.w.zero_()
+        self.acc.add_(self.r.sum())
+
+
 def time_steps(L, torch, stream, steps, warmup, flush):
     """Per-step CUDA-event time (ms) of `steps` single LBM steps, each after an L2 flush."""
     with torch.cuda.stream(stream):
         for _ in range(warmup):
             if flush is not None:
-                flush.zero_()
+                flush()
             L.step(1, flags=0)
         stream.synchronize()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         for s, e in evs:
             if flush is not None:
-                flush.zero_()
+                flush()
             s.record(stream)
             L.step(1, flags=0)
             e.record(stream)
@@ -164,6 +185,76 @@ def run_cpu_oracle(n, steps, threads):
     dt = time.perf_counter() - t0
     _, u, _ = o.moments()
     return u, (n * n * (steps - 1)) / dt / 1e6, dt
+
+
+def bench_ensemble(args, torch, stream, device, hbm):
+    """Batched ensemble: `args.ens_count` lid-driven cavities (sides uniform in
+    {64, ..., 768}, Re log-uniform in [100, 5000], seed 0), D2Q9 MRT, advanced
+    by one persistent launch per step replayed from CUDA graphs, tile shape
+    from the autotuner.  Aggregate MLUPS for FP16-offset and FP32 storage,
+    and the relative L2 velocity error against the FP64 oracle of the
+    smallest instances (a lattice's result does not depend on the batch it
+    runs in: the batched kernel is bit-identical to stepping it alone)."""
+    import cases as C
+    import lbmx
+    ens = C.ensemble(count=args.ens_count)
+    nodes = sum(s * s for s, _, _ in ens)
+
+    def build(storage, members):
+        Ls = []
+        for side, _, nu in members:
+            c = C.ensemble_cavity(side, nu)
+            L = lbmx.Lattice(side, side, op=c["op"], omega=c["omega"], S=c["S"], storage=storage,
+                             wall_u=c["wall_u"], device=device, stream=stream.cuda_stream)
+            L.set_flags(c["flags"])
+            L.init(np.ones((side, side), np.float32), np.zeros((2, side, side), np.float32))
+            Ls.append(L)
+        return Ls
+
+    out = {"workload": "%d lid-driven cavities, sides uniform in {64,96,...,768}, Re log-uniform [100,5000], "
+                       "seed 0, D2Q9 MRT, lid 0.1" % len(ens), "nodes": int(nodes)}
+    for storage in (1, 0):
+        Ls = build(storage, ens)
+        B = lbmx.Batch(Ls)
+        cfg = B.autotune(trial_steps=4)
+        B.step(max(args.warmup, 3) * 2, flags=0)
+        B.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        B.step(args.ens_steps, flags=0)
+        e1.record(stream)
+        B.step(1, flags=lbmx.STEP_STORE_MOMENTS)
+        B.synchronize()
+        ms = e0.elapsed_time(e1) / args.ens_steps
+        bad = 0
+        for L in Ls:
+            r, _, _ = L.moments()
+            bad += int(not np.isfinite(r).all())
+        a = BYTES_PER_LU[storage] * nodes / (ms * 1e-3) / 1e9
+        out[STORAGE_NAME[storage]] = {"MLUPS": round(nodes / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms, 4),
+                                      "achieved_GBs": round(a, 1), "frac": round(a / hbm, 4),
+                                      "autotuned": cfg, "nonfinite_instances": bad,
+                                      "timed_steps": args.ens_steps}
+        B.close()
+        del Ls, B
+    out["f16_speedup_vs_f32"] = round(out["f16_offset"]["MLUPS"] / out["f32"]["MLUPS"], 3)
+    # per-instance error of the smallest instances against the FP64 oracle
+    sample = sorted(range(len(ens)), key=lambda i: (ens[i][0], i))[: args.ens_err_count]
+    members = [ens[i] for i in sample]
+    Ls = build(1, members)
+    B = lbmx.Batch(Ls)
+    B.step(args.ens_err_steps)
+    errs = []
+    for (side, re, nu), L in zip(members, Ls):
+        o = C.make_oracle(C.ensemble_cavity(side, nu))
+        o.step(args.ens_err_steps)
+        _, uo, _ = o.moments()
+        _, ul, _ = L.moments()
+        errs.append({"instance": sample[len(errs)], "side": side, "Re": round(re, 1),
+                     "l2_u_err_vs_fp64": l2_error(ul, uo)})
+    out["l2_err_sample"] = {"storage": "f16_offset", "steps": args.ens_err_steps, "instances": errs,
+                            "max": max(e["l2_u_err_vs_fp64"] for e in errs)}
+    return out
 
 
 def bench_reference(args, rank, world):
@@ -208,6 +299,10 @@ def main():
     ap.add_argument("--hbm-size", type=int, default=8192)
     ap.add_argument("--err-steps", type=int, default=200)
     ap.add_argument("--ref-lbm-steps", type=int, default=5)
+    ap.add_argument("--ens-count", type=int, default=512)
+    ap.add_argument("--ens-steps", type=int, default=64)
+    ap.add_argument("--ens-err-count", type=int, default=6)
+    ap.add_argument("--ens-err-steps", type=int, default=1000)
     ap.add_argument("--quick", action="store_true", help="main number only (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -233,7 +328,7 @@ def main():
     nodes = n * n
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    flush = L2Flush(torch)
 
     def lattice(storage, size=n):
         c = cavity_case(size)
@@ -261,7 +356,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "lid-driven cavity %dx%d, D2Q9 MRT, lid 0.1 half-way moving wall, Re 1000" % (n, n),
-                   "nodes": nodes, "storage": "f32", "l2": "flushed: 256 MB write before every timed step",
+                   "nodes": nodes, "storage": "f32", "l2": "flushed before every timed step: 256 MB write, then 256 MB read of a second buffer",
                    "parallelism": "replica per GPU" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": None,
@@ -348,6 +443,8 @@ def main():
             "f16_offset": {"MLUPS": round(hn * hn / (float(th16.mean()) * 1e-3) / 1e6, 1),
                            "achieved_GBs": round(a16, 1), "frac": round(a16 / hbm, 4)},
         }
+        # ---- batched ensemble (many lattices, one persistent launch per step)
+        line["ensemble"] = bench_ensemble(args, torch, stream, local, hbm)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -96,7 +96,7 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.forced = (h->p.body_fx != 0.0f || h->p.body_fy != 0.0f || h->force != nullptr || h->nm > 0) ? 1 : 0;
     a.special_units = h->special_units;
     a.nspecial = h->nspecial;
-    a.special_blocks = h->special_blocks;
+    a.special_chunks = h->special_chunks;
     a.special_bits = h->special_bits;
     a.tiles_x = h->tiles_x;
     a.tiles_y = h->tiles_y;
@@ -149,16 +149,16 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
         LBMX_CUDA(h, cudaMemcpy(h->special_bits, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
     h->nspecial = (int)units.size();
-    h->special_blocks = (h->nspecial + kStepThreads - 1) / kStepThreads;
+    h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
     h->tiles_x = (g.nx + kStageW - 1) / kStageW;
     h->tiles_y = (g.ny - 2 + kStageH - 1) / kStageH;
-    // two persistent interior CTAs per SM walk the tiles
-    const long long tiles = (long long)h->tiles_x * h->tiles_y;
-    h->num_ctas = (int)std::min<long long>(tiles, 2LL * h->num_sms);
-    // claim tiles in chunks of about 1/16 of a CTA's share: few atomics on
-    // large lattices, still one tile at a time on small ones
-    h->tile_chunk = (int)std::max<long long>(1, tiles / (16LL * h->num_ctas));
-    const long long blocks = h->special_blocks + h->num_ctas;
+    // two persistent CTAs per SM walk the work list
+    const long long items = (long long)h->tiles_x * h->tiles_y + h->special_chunks;
+    h->num_ctas = (int)std::max<long long>(1, std::min<long long>(items, 2LL * h->num_sms));
+    // claim items in chunks of about 1/16 of a CTA's share: few atomics on
+    // large lattices, still one item at a time on small ones
+    h->tile_chunk = (int)std::max<long long>(1, items / (16LL * h->num_ctas));
+    const long long blocks = h->num_ctas;
     if (blocks > h->partial_cap) {
         cudaFree(h->partials);
         h->partials = nullptr;

@@ -25,6 +25,7 @@ struct lbmx_batch {
     std::vector<lbmx_handle*> lat;
     int device = 0, storage = 0, op = 0, num_sms = 1;
     cudaStream_t stream = nullptr;
+    bool own_stream = false;  // false: every lattice runs on this one stream
     lbmx_batch_config cfg{128, 4, 2, 1, 16};
     // device state of the current configuration
     StepArgs* d_args = nullptr;        // [kVariants][2 parities][count]
@@ -90,7 +91,7 @@ static lbmx_status refresh(lbmx_batch* b) {
         StepArgs a = base_args(h);
         a.tiles_x = (h->g.nx + tw - 1) / tw;
         a.tiles_y = (h->g.ny - 2 + th - 1) / th;
-        a.special_blocks = 0;
+        a.special_chunks = 0;
         a.num_ctas = 0;
         a.tile_counter = nullptr;
         a.done_counter = nullptr;
@@ -126,7 +127,7 @@ static lbmx_status refresh(lbmx_batch* b) {
     for (int l = 0; l < n; l++) {
         if (!encode_population_map(b->lat[l], &maps[l], tw, th))
             return bfail(b, LBMX_ERR_CUDA, "lbmx_batch: cannot build the TMA descriptor of lattice %d", l);
-        const int chunks = (b->lat[l]->nspecial + kSpecialChunk - 1) / kSpecialChunk;
+        const int chunks = (2 * b->lat[l]->nspecial + kSpecialChunk - 1) / kSpecialChunk;
         for (int c = 0; c < chunks; c++) items.push_back(make_int2(l, -(c + 1)));
     }
     for (int l = 0; l < n; l++) {
@@ -249,6 +250,7 @@ static lbmx_status check_lattices(lbmx_batch* b) {
 }
 
 static lbmx_status wait_lattices(lbmx_batch* b) {
+    if (!b->own_stream) return LBMX_OK;
     for (size_t i = 0; i < b->streams.size(); i++) {
         BATCH_CUDA(b, cudaEventRecord(b->stream_events[i], b->streams[i]));
         BATCH_CUDA(b, cudaStreamWaitEvent(b->stream, b->stream_events[i], 0));
@@ -257,6 +259,7 @@ static lbmx_status wait_lattices(lbmx_batch* b) {
 }
 
 static lbmx_status release_lattices(lbmx_batch* b) {
+    if (!b->own_stream) return LBMX_OK;
     BATCH_CUDA(b, cudaEventRecord(b->end_event, b->stream));
     for (cudaStream_t s : b->streams) BATCH_CUDA(b, cudaStreamWaitEvent(s, b->end_event, 0));
     return LBMX_OK;
@@ -269,13 +272,16 @@ void lbmx_batch_destroy(lbmx_batch* b) {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(b->device);
-    if (b->stream) cudaStreamSynchronize(b->stream);
+    // a borrowed stream belongs to the lattices and may already be gone:
+    // wait for the device instead of touching it
+    if (b->own_stream && b->stream) cudaStreamSynchronize(b->stream);
+    else cudaDeviceSynchronize();
     drop_graphs(b);
     cudaFree(b->d_args); cudaFree(b->d_tmaps); cudaFree(b->d_items);
     cudaFree(b->counter); cudaFree(b->done); cudaFree(b->error_word);
     for (cudaEvent_t e : b->stream_events) cudaEventDestroy(e);
     if (b->end_event) cudaEventDestroy(b->end_event);
-    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     cudaSetDevice(cur);
     delete b;
 }
@@ -317,17 +323,24 @@ lbmx_status lbmx_batch_create(lbmx_handle* const* lattices, int32_t count, lbmx_
         lbmx_batch_destroy(b);
         return code;
     };
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->end_event, cudaEventDisableTiming) != cudaSuccess)
-        return cleanup(LBMX_ERR_CUDA, "cannot create the batch stream");
     for (lbmx_handle* h : b->lat)
-        if (std::find(b->streams.begin(), b->streams.end(), h->stream) == b->streams.end()) {
+        if (std::find(b->streams.begin(), b->streams.end(), h->stream) == b->streams.end())
+            b->streams.push_back(h->stream);
+    if (b->streams.size() == 1) {
+        // one stream for every lattice: the batch runs on it, no cross-stream waits
+        b->stream = b->streams[0];
+    } else {
+        b->own_stream = true;
+        if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->end_event, cudaEventDisableTiming) != cudaSuccess)
+            return cleanup(LBMX_ERR_CUDA, "cannot create the batch stream");
+        for (size_t i = 0; i < b->streams.size(); i++) {
             cudaEvent_t e = nullptr;
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
                 return cleanup(LBMX_ERR_CUDA, "cannot create an event");
-            b->streams.push_back(h->stream);
             b->stream_events.push_back(e);
         }
+    }
     if (cudaMalloc((void**)&b->counter, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void**)&b->done, sizeof(unsigned int)) != cudaSuccess ||
         cudaMalloc((void**)&b->error_word, sizeof(unsigned int)) != cudaSuccess)

@@ -110,13 +110,7 @@ __global__ void __launch_bounds__(kThreads, 2) batch_step_kernel(const BatchArgs
                         interior_unit<T, OP, P, TW, TH>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
                 }
             } else {
-                const int u = (-it.y - 1) * kSpecialChunk + tid;
-                if (u < a.nspecial) {
-                    const int off = a.special_units[u];
-                    const int y = off / a.g.pitch, x0 = off - y * a.g.pitch;
-#pragma unroll 1
-                    for (int x = x0; x < x0 + 2 && x < a.g.nx; x++) general_node<T, OP>(a, x, y, v);
-                }
+                special_chunk<T, OP>(a, -it.y - 1, tid, v);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);

@@ -50,7 +50,7 @@ struct lbmx_handle {
     std::vector<uint8_t> flags_host;  // pitched copy of the flags (empty: all fluid)
     int* special_units = nullptr;
     uint32_t* special_bits = nullptr;
-    int nspecial = 0, special_blocks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
+    int nspecial = 0, special_chunks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
     void* f_alloc = nullptr;  // population allocation including the guard elements
     unsigned long long* tile_counter = nullptr;
     unsigned int* done_counter = nullptr;

@@ -54,7 +54,7 @@ struct StepArgs {
     // work split of the step kernel (lbmx_kernels.cuh)
     const int* special_units;      // unit offsets y*pitch + x0 handled by the general path
     int nspecial;
-    int special_blocks;            // leading CTAs that take the special units
+    int special_chunks;            // work items of kSpecialChunk special nodes that lead the work list
     const uint32_t* special_bits;  // 1 bit per unit for special units off the perimeter, or nullptr
     int tiles_x, tiles_y;          // interior tiles (kStageW x kStageH nodes, rows 1..ny-2)
     int num_ctas;                  // persistent CTAs that walk the interior tiles
@@ -132,7 +132,7 @@ constexpr int kStepThreads = 288;  // 8 consumer warps + 1 producer warp
 constexpr int kConsumerWarps = 8;
 constexpr int kStageW = 128;
 constexpr int kStageH = 4;
-constexpr int kSpecialChunk = kConsumerWarps * 32;  // special units per batched work item
+constexpr int kSpecialChunk = kConsumerWarps * 32;  // special nodes per work item (one per consumer thread)
 // guard elements before and after the population planes: staged row copies
 // reach one 16-byte chunk beyond a row segment on each side
 constexpr int kGuardElems = 64;

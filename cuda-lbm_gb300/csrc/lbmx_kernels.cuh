@@ -9,12 +9,12 @@
 //                moments, force correction, collision, store in place.
 //
 // The step kernel works on "units" of two x-neighbouring nodes (x0 even).
-// Its first `special_blocks` CTAs take the units listed as special -- the
-// domain perimeter and every unit holding a flagged or IBM-forced node --
-// one unit per thread through the general per-node path.  The other CTAs are
-// persistent: each walks interior tiles of 128 x 4 nodes (rows 1..ny-2),
-// staged into shared memory by bulk asynchronous copies, one unit per
-// thread, and skips the special units.  An interior unit needs no boundary,
+// Units listed as special -- the domain perimeter and every unit holding a
+// flagged or IBM-forced node -- go through the general per-node path, one
+// node per thread, in chunks of 256 nodes that lead the work list.  Interior
+// tiles of 128 x 4 nodes (rows 1..ny-2) follow, staged into shared memory by
+// bulk asynchronous copies, one unit per thread, skipping the special units.
+// Every CTA is persistent and claims items from one counter.  An interior unit needs no boundary,
 // wrap or flag logic, reads its two nodes as one 64-bit (FP32) or 32-bit
 // (16-bit) shared-memory access wherever the pair stays aligned, collides
 // both nodes at once in packed FP32x2 arithmetic and stores in place.  The
@@ -339,91 +339,110 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     }
 }
 
+// One chunk of special nodes: consumer thread t takes node `first + t` of
+// the special-unit list (two nodes per unit).
+template <typename T, int OP>
+__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, double v[6]) {
+    const int k = chunk * kSpecialChunk + tid;
+    if (k >= 2 * a.nspecial) return;
+    const int off = a.special_units[k >> 1];
+    const int y = off / a.g.pitch, x = off - y * a.g.pitch + (k & 1);
+    if (x < a.g.nx) general_node<T, OP>(a, x, y, v);
+}
+
 template <typename T, int OP, int P>
 __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
+    // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
+    // work item from a global counter; for an interior tile it bulk-copies
+    // the tile into the ring), warps 0-7 consume.  Items 0..special_chunks-1
+    // are chunks of special nodes (general path, one node per consumer
+    // thread, nothing staged) so the boundary work spreads over every SM;
+    // the interior tiles follow.  full[s] completes when a stage's bytes have
+    // landed (or at once for a special chunk); empty[s] when all eight
+    // consumer warps are done with it.
     using St = Staging<T>;
     double v[6] = {0, 0, 0, 0, 0, 0};
     const int tid = threadIdx.x;
-    if ((int)blockIdx.x < a.special_blocks) {
-        const int u = blockIdx.x * kThreads + tid;
-        if (u < a.nspecial) {
-            const int off = a.special_units[u];
-            const int y = off / a.g.pitch, x0 = off - y * a.g.pitch;
-#pragma unroll 1
-            for (int x = x0; x < x0 + 2 && x < a.g.nx; x++) general_node<T, OP>(a, x, y, v);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* bufs = reinterpret_cast<T*>(smem_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + St::BUF_BYTES);
+    uint64_t* empty = full + St::NST;
+    volatile int* item_id = reinterpret_cast<volatile int*>(empty + St::NST);
+    const int nchunks = a.special_chunks;
+    const int nitems = nchunks + a.tiles_x * a.tiles_y;
+    const int warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int s = 0; s < St::NST; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
         }
-    } else {
-        // Persistent interior CTA, warp-specialised: warp 8 produces (claims
-        // the next tile from a global counter and bulk-copies it into the
-        // ring), warps 0-7 consume.  full[s] completes when a stage's bytes
-        // have landed; empty[s] when all eight consumer warps are done with it.
-        extern __shared__ __align__(128) unsigned char smem_raw[];
-        T* bufs = reinterpret_cast<T*>(smem_raw);
-        uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + St::BUF_BYTES);
-        uint64_t* empty = full + St::NST;
-        volatile int* tile_id = reinterpret_cast<volatile int*>(empty + St::NST);
-        const int ntiles = a.tiles_x * a.tiles_y;
-        const int warp = tid >> 5, lane = tid & 31;
-        if (tid == 0) {
-            for (int s = 0; s < St::NST; s++) {
-                mbar_init(&full[s], 1);
-                mbar_init(&empty[s], kConsumerWarps);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == kConsumerWarps) {
+        // producer: claims `tile_chunk` consecutive items per atomic
+        int k = 0;
+        bool failed = false;
+        int next = 0, left = 0;
+        for (;; k++) {
+            const int s = k % St::NST;
+            if (k >= St::NST && !mbar_wait(&empty[s], (unsigned)(((k / St::NST) - 1) & 1), kWaitLimit)) {
+                if (lane == 0) atomicOr(a.error_word, 2u);
+                failed = true;
+                break;
             }
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        __syncthreads();
-        if (warp == kConsumerWarps) {
-            // producer: claims `tile_chunk` consecutive tiles per atomic
-            int k = 0;
-            bool failed = false;
-            int next = 0, left = 0;
-            for (;; k++) {
-                const int s = k % St::NST;
-                if (k >= St::NST && !mbar_wait(&empty[s], (unsigned)(((k / St::NST) - 1) & 1), kWaitLimit)) {
-                    if (lane == 0) atomicOr(a.error_word, 2u);
-                    failed = true;
-                    break;
-                }
-                if (left == 0) {
-                    int base = 0;
-                    if (lane == 0) base = (int)atomicAdd(a.tile_counter, (unsigned long long)a.tile_chunk);
-                    next = __shfl_sync(0xffffffffu, base, 0);
-                    left = a.tile_chunk;
-                }
-                const int tile = next++;
-                left--;
-                if (tile >= ntiles) {
-                    if (lane == 0) {
-                        tile_id[s] = -1;
-                        mbar_arrive(&full[s]);
-                    }
-                    break;
-                }
+            if (left == 0) {
+                int base = 0;
+                if (lane == 0) base = (int)atomicAdd(a.tile_counter, (unsigned long long)a.tile_chunk);
+                next = __shfl_sync(0xffffffffu, base, 0);
+                left = a.tile_chunk;
+            }
+            const int item = next++;
+            left--;
+            if (item >= nitems) {
                 if (lane == 0) {
-                    tile_id[s] = tile;
-                    fence_proxy_async_smem();
-                    mbar_expect_tx(&full[s], St::STAGE_BYTES);
+                    item_id[s] = -1;
+                    mbar_arrive(&full[s]);
+                }
+                break;
+            }
+            if (item < nchunks) {
+                if (lane == 0) {
+                    item_id[s] = item;
+                    mbar_arrive(&full[s]);
                 }
                 __syncwarp();
-                stage_issue<T, P>(a, &tmap, tile, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+                continue;
             }
-            // On the normal path the consumers have waited for every fill.  If
-            // they stopped releasing stages, let the fills still unconsumed
-            // (at most one per stage) land before the CTA exits (bounded).
-            if (failed && lane == 0)
-                for (int j = max(0, k - St::NST); j < k; j++)
-                    mbar_wait(&full[j % St::NST], (unsigned)((j / St::NST) & 1), kWaitLimit);
-        } else {
-            // consumers
-            const int lx = tid % (St::TW / 2), r = tid / (St::TW / 2);
-            for (int i = 0;; i++) {
-                const int s = i % St::NST;
-                if (!mbar_wait(&full[s], (unsigned)((i / St::NST) & 1), kWaitLimit)) {
-                    if (lane == 0) atomicOr(a.error_word, 2u);
-                    break;
-                }
-                const int tile = tile_id[s];
-                if (tile < 0) break;
+            if (lane == 0) {
+                item_id[s] = item;
+                fence_proxy_async_smem();
+                mbar_expect_tx(&full[s], St::STAGE_BYTES);
+            }
+            __syncwarp();
+            stage_issue<T, P>(a, &tmap, item - nchunks, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+        }
+        // On the normal path the consumers have waited for every fill.  If
+        // they stopped releasing stages, let the fills still unconsumed
+        // (at most one per stage) land before the CTA exits (bounded).
+        if (failed && lane == 0)
+            for (int j = max(0, k - St::NST); j < k; j++)
+                mbar_wait(&full[j % St::NST], (unsigned)((j / St::NST) & 1), kWaitLimit);
+    } else {
+        // consumers
+        const int lx = tid % (St::TW / 2), r = tid / (St::TW / 2);
+        for (int i = 0;; i++) {
+            const int s = i % St::NST;
+            if (!mbar_wait(&full[s], (unsigned)((i / St::NST) & 1), kWaitLimit)) {
+                if (lane == 0) atomicOr(a.error_word, 2u);
+                break;
+            }
+            const int item = item_id[s];
+            if (item < 0) break;
+            if (item < nchunks) {
+                special_chunk<T, OP>(a, item, tid, v);
+            } else {
+                const int tile = item - nchunks;
                 const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
                 const int x0 = tx * St::TW + 2 * lx, y = 1 + ty * St::TH + r;
                 bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
@@ -432,14 +451,13 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, con
                     live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
                 }
                 if (live) interior_unit<T, OP, P>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
-                __syncwarp();
-                if (lane == 0)
-                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&empty[s])) : "memory");
             }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s]);
         }
     }
     if (a.partials) block_sums(a, v, (long long)a.g.nx * a.g.ny);
-    // the last CTA to finish re-arms the tile counter for the next launch
+    // the last CTA to finish re-arms the item counter for the next launch
     if (tid == 0) {
         __threadfence();
         if (atomicAdd(a.done_counter, 1u) == gridDim.x - 1) {
@@ -665,7 +683,7 @@ static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tma
 
 template <typename T>
 cudaError_t launch_step(const StepArgs& a, const CUtensorMap& tmap, int op, cudaStream_t s) {
-    const unsigned grid = (unsigned)(a.special_blocks + a.num_ctas);
+    const unsigned grid = (unsigned)a.num_ctas;
 #define LBMX_STEP_CASE(OPV)                                                    \
     return a.parity ? launch_step_variant<T, OPV, 1>(a, tmap, grid, s)         \
                     : launch_step_variant<T, OPV, 0>(a, tmap, grid, s);
@@ -681,7 +699,7 @@ cudaError_t launch_step(const StepArgs& a, const CUtensorMap& tmap, int op, cuda
 template <typename T>
 cudaError_t launch_opt_prepass(const StepArgs& a, cudaStream_t s) {
     // as many CTAs as the step kernel, so the FP64 partials buffer fits both
-    opt_prepass_kernel<T><<<a.special_blocks + a.num_ctas, kThreads, 0, s>>>(a);
+    opt_prepass_kernel<T><<<a.num_ctas, kThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 

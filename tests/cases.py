@@ -135,11 +135,11 @@ def make_oracle(c, precision="f64"):
     return o
 
 
-def make_lattice(c, storage=0, options=0):
+def make_lattice(c, storage=0, options=0, stream=None):
     import lbmx
     L = lbmx.Lattice(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], periodic=c["periodic"],
                      storage=storage, quirks=c["quirks"], options=options, u_bc=c["u_bc"],
-                     wall_u=c["wall_u"], rho_out=c["rho_out"])
+                     wall_u=c["wall_u"], rho_out=c["rho_out"], stream=stream)
     L.set_flags(c["flags"])
     L.init(np.asarray(c["rho"], np.float32), np.asarray(c["u"], np.float32),
            None if c["force"] is None else np.asarray(c["force"], np.float32))

@@ -59,14 +59,18 @@ def test_batch_matches_lattices_stepped_alone(op, storage, tile_w, tile_h, ctas,
     B.close()
 
 
-def test_batch_reference_quirks():
+def test_batch_reference_quirks_on_a_shared_stream():
+    # every lattice on one stream: the batch runs on it directly
+    torch = pytest.importorskip("torch")
+    s = torch.cuda.Stream()
     cs = mixed_cases(C.MRT, quirks=C.QUIRKS_REFERENCE)
     alone = [C.make_lattice(c) for c in cs]
-    batched = [C.make_lattice(c) for c in cs]
+    batched = [C.make_lattice(c, stream=s.cuda_stream) for c in cs]
     for L in alone:
         L.step(17)
     B = lbmx.Batch(batched)
-    B.step(17)
+    B.step(9)
+    B.step(8)
     assert_same(alone, batched)
 
 
