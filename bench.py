@@ -304,6 +304,8 @@ def main():
     ap.add_argument("--ens-err-count", type=int, default=6)
     ap.add_argument("--ens-err-steps", type=int, default=1000)
     ap.add_argument("--quick", action="store_true", help="main number only (profiling runs)")
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16_offset", "bf16_offset"],
+                    help="storage of the main lattice with --quick (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -339,7 +341,8 @@ def main():
         return L
 
     # ---- headline: FP32, L2 flushed before every timed step
-    L = lattice(0)
+    main_storage = {v: k for k, v in STORAGE_NAME.items()}[args.storage] if args.quick else 0
+    L = lattice(main_storage)
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
@@ -350,17 +353,17 @@ def main():
         dist.barrier()
     ms = max_over_ranks(float(t.mean()), dist, "cuda")
     mlups = aggregate_mlups(nodes, ms, world)
-    achieved = BYTES_PER_LU[0] * nodes / (float(t.mean()) * 1e-3) / 1e9
+    achieved = BYTES_PER_LU[main_storage] * nodes / (float(t.mean()) * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "lid-driven cavity %dx%d, D2Q9 MRT, lid 0.1 half-way moving wall, Re 1000" % (n, n),
-                   "nodes": nodes, "storage": "f32", "l2": "flushed before every timed step: 256 MB write, then 256 MB read of a second buffer",
+                   "nodes": nodes, "storage": STORAGE_NAME[main_storage], "l2": "flushed before every timed step: 256 MB write, then 256 MB read of a second buffer",
                    "parallelism": "replica per GPU" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": None,
-                     "algorithmic_bytes_per_lu": BYTES_PER_LU[0], "peak_kind": peak_kind + " burst (hbm_gbs)"},
+                     "algorithmic_bytes_per_lu": BYTES_PER_LU[main_storage], "peak_kind": peak_kind + " burst (hbm_gbs)"},
         "gpu_launches": int(args.steps),
         "clocks": clk.summary(),
     }

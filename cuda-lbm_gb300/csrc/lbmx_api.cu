@@ -152,9 +152,13 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
     h->tiles_x = (g.nx + kStageW - 1) / kStageW;
     h->tiles_y = (g.ny - 2 + kStageH - 1) / kStageH;
-    // two persistent CTAs per SM walk the work list
+    // persistent CTAs walk the work list: kCtasPerSm per SM on large
+    // lattices; two per SM when each CTA would get fewer than 16 items (a
+    // small lattice is latency-bound and gains more from fuller CTAs than
+    // from more warps)
     const long long items = (long long)h->tiles_x * h->tiles_y + h->special_chunks;
-    h->num_ctas = (int)std::max<long long>(1, std::min<long long>(items, 2LL * h->num_sms));
+    const int per_sm = items >= 16LL * kCtasPerSm * h->num_sms ? kCtasPerSm : 2;
+    h->num_ctas = (int)std::max<long long>(1, std::min<long long>(items, (long long)per_sm * h->num_sms));
     // claim items in chunks of about 1/16 of a CTA's share: few atomics on
     // large lattices, still one item at a time on small ones
     h->tile_chunk = (int)std::max<long long>(1, items / (16LL * h->num_ctas));

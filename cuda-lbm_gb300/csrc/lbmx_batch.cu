@@ -26,7 +26,7 @@ struct lbmx_batch {
     int device = 0, storage = 0, op = 0, num_sms = 1;
     cudaStream_t stream = nullptr;
     bool own_stream = false;  // false: every lattice runs on this one stream
-    lbmx_batch_config cfg{128, 4, 2, 1, 16};
+    lbmx_batch_config cfg{128, 4, kCtasPerSm, 1, 16};
     // device state of the current configuration
     StepArgs* d_args = nullptr;        // [kVariants][2 parities][count]
     CUtensorMap* d_tmaps = nullptr;    // [count]
@@ -75,7 +75,7 @@ static void drop_graphs(lbmx_batch* b) {
 
 static bool valid_config(const lbmx_batch_config& c) {
     const bool shape = (c.tile_w == 64 && c.tile_h == 8) || (c.tile_w == 128 && (c.tile_h == 4 || c.tile_h == 8));
-    return shape && (c.ctas_per_sm == 1 || c.ctas_per_sm == 2) &&
+    return shape && (c.ctas_per_sm >= 1 && c.ctas_per_sm <= kCtasPerSm) &&
            c.chunk >= 1 && c.chunk <= 64 && c.graph_steps >= 0 && c.graph_steps <= 64 && c.graph_steps % 2 == 0;
 }
 
@@ -467,7 +467,7 @@ lbmx_status lbmx_batch_autotune(lbmx_batch* b, int32_t trial_steps, lbmx_batch_c
     static const int shapes[3][2] = {{64, 8}, {128, 4}, {128, 8}};
     static const int chunks[3] = {1, 2, 4};
     for (int ti = 0; ti < 3 && st == LBMX_OK; ti++)
-        for (int c = 1; c <= 2 && st == LBMX_OK; c++)
+        for (int c = 1; c <= kCtasPerSm && st == LBMX_OK; c++)
             for (int ki = 0; ki < 3 && st == LBMX_OK; ki++) {
                 // trials launch directly: one launch per step for every
                 // candidate, so graphs would not change the ranking

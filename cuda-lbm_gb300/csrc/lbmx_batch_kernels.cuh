@@ -19,13 +19,13 @@
 namespace lbmx {
 
 template <typename T, int OP, int P, int TW, int TH>
-__global__ void __launch_bounds__(kThreads, 2) batch_step_kernel(const BatchArgs b) {
+__global__ void __launch_bounds__(kThreads, (TW * TH > kStageW * kStageH) ? 2 : kCtasPerSm) batch_step_kernel(const BatchArgs b) {
     using St = Staging<T, TW, TH>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* bufs = reinterpret_cast<T*>(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + St::BUF_BYTES);
     uint64_t* empty = full + St::NST;
-    volatile int* item_id = reinterpret_cast<volatile int*>(empty + St::NST);
+    int4* slot = reinterpret_cast<int4*>(empty + St::NST);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int s = 0; s < St::NST; s++) {
@@ -55,29 +55,31 @@ __global__ void __launch_bounds__(kThreads, 2) batch_step_kernel(const BatchArgs
             left--;
             if (item >= b.nitems) {
                 if (lane == 0) {
-                    item_id[s] = -1;
+                    put_slot(&slot[s], -1, 0, 0, 0);
                     mbar_arrive(&full[s]);
                 }
                 break;
             }
             const int2 it = b.items[item];
             if (it.y < 0) {
-                // a chunk of special units: nothing to stage
+                // a chunk of special nodes: nothing to stage
                 if (lane == 0) {
-                    item_id[s] = item;
+                    put_slot(&slot[s], -2 - (-it.y - 1), 0, 0, it.x);
                     mbar_arrive(&full[s]);
                 }
                 __syncwarp();
                 continue;
             }
             const StepArgs& a = b.lat[it.x];
+            const int ty = it.y / a.tiles_x, tx = it.y - ty * a.tiles_x;
+            const int x0 = tx * TW, y0 = 1 + ty * TH;
             if (lane == 0) {
-                item_id[s] = item;
+                put_slot(&slot[s], it.y, x0, y0, it.x);
                 fence_proxy_async_smem();
                 mbar_expect_tx(&full[s], St::STAGE_BYTES);
             }
             __syncwarp();
-            stage_issue<T, P, TW, TH>(a, b.tmaps + it.x, it.y, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+            stage_issue<T, P, TW, TH>(a, b.tmaps + it.x, x0, y0, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
         }
         if (failed && lane == 0)
             for (int j = max(0, k - St::NST); j < k; j++)
@@ -91,16 +93,14 @@ __global__ void __launch_bounds__(kThreads, 2) batch_step_kernel(const BatchArgs
                 if (lane == 0) atomicOr(b.error_word, 2u);
                 break;
             }
-            const int item = item_id[s];
-            if (item < 0) break;
-            const int2 it = b.items[item];
-            const StepArgs& a = b.lat[it.x];
-            if (it.y >= 0) {
-                const int ty = it.y / a.tiles_x, tx = it.y - ty * a.tiles_x;
-                const int x0 = tx * TW + 2 * lx;
+            const int4 sl = get_slot(&slot[s]);
+            if (sl.x == -1) break;
+            const StepArgs& a = b.lat[sl.w];
+            if (sl.x >= 0) {
+                const int x0 = sl.y + 2 * lx;
 #pragma unroll
                 for (int r = r0; r < TH; r += St::ROWS) {
-                    const int y = 1 + ty * TH + r;
+                    const int y = sl.z + r;
                     bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
                     if (live && a.special_bits) {
                         const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, 2) batch_step_kernel(const BatchArgs
                         interior_unit<T, OP, P, TW, TH>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
                 }
             } else {
-                special_chunk<T, OP>(a, -it.y - 1, tid, v);
+                special_chunk<T, OP>(a, -2 - sl.x, tid, v);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);

@@ -64,13 +64,31 @@ __device__ __forceinline__ float vpos_or(float a, float alt) { return a > 0.f ? 
 // O(|u|) instead of O(1) and so keeps 10 (FP16) or 7 (BF16) significant bits
 // for the part of f that carries the flow.
 template <typename T> struct Store;
+//
+// ld/st/ld2/st2 convert between f and the stored form; ldr/str/ld2r/st2r move
+// the stored value itself (f for FP32, f - w for the 16-bit forms), for code
+// that computes with offsets directly (kOffset<T>).
+template <typename T>
+constexpr bool kOffset = sizeof(T) == 2;
 template <> struct Store<float> {
+    static __device__ __forceinline__ float ldr(const float* p) { return *p; }
+    static __device__ __forceinline__ float2 ld2r(const float* p) { return *reinterpret_cast<const float2*>(p); }
+    static __device__ __forceinline__ void str(float* p, float v) { *p = v; }
+    static __device__ __forceinline__ void st2r(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
     static __device__ __forceinline__ float ld(const float* p, float) { return *p; }
     static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
     static __device__ __forceinline__ float2 ld2(const float* p, float) { return *reinterpret_cast<const float2*>(p); }
     static __device__ __forceinline__ void st2(float* p, float2 v, float) { *reinterpret_cast<float2*>(p) = v; }
 };
 template <> struct Store<__half> {
+    static __device__ __forceinline__ float ldr(const __half* p) { return __half2float(*p); }
+    static __device__ __forceinline__ float2 ld2r(const __half* p) {
+        return __half22float2(*reinterpret_cast<const __half2*>(p));
+    }
+    static __device__ __forceinline__ void str(__half* p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ void st2r(__half* p, float2 v) {
+        *reinterpret_cast<__half2*>(p) = __float22half2_rn(v);
+    }
     static __device__ __forceinline__ float ld(const __half* p, float w) { return w + __half2float(*p); }
     static __device__ __forceinline__ void st(__half* p, float v, float w) { *p = __float2half_rn(v - w); }
     static __device__ __forceinline__ float2 ld2(const __half* p, float w) {
@@ -82,6 +100,14 @@ template <> struct Store<__half> {
     }
 };
 template <> struct Store<__nv_bfloat16> {
+    static __device__ __forceinline__ float ldr(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+    static __device__ __forceinline__ float2 ld2r(const __nv_bfloat16* p) {
+        return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+    }
+    static __device__ __forceinline__ void str(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void st2r(__nv_bfloat16* p, float2 v) {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn(v);
+    }
     static __device__ __forceinline__ float ld(const __nv_bfloat16* p, float w) { return w + __bfloat162float(*p); }
     static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
     static __device__ __forceinline__ float2 ld2(const __nv_bfloat16* p, float w) {
@@ -389,10 +415,13 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
 // ---------------------------------------------------------------- collision
 // All operators take the post-stream (post-boundary) populations f, the
 // density, the force-corrected velocity and the force, and overwrite f with
-// the post-collision populations.
+// the post-collision populations.  With OFS, f holds offsets f - w_q on entry
+// and on exit (rho is the full density): the weights' own moments are folded
+// into the equilibrium constants, so 16-bit storage needs no per-population
+// add on load or store.
 
 // BGK<2>::apply with Guo forcing -- BGK.cuh:15-39
-template <typename R>
+template <typename R, bool OFS = false>
 __device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R Fy, float omega, bool forced) {
     const R uu = fma(ux, ux, uy * uy);
     const R one = splat(1.0f, ux);
@@ -407,7 +436,8 @@ __device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R F
         else cu = fma(cx, ux, cy * uy);
         // feq = w rho (1 + 3cu + 4.5cu^2 - 1.5uu)
         const R br = fma(cu, fma(splat(4.5f, ux), cu, splat(3.0f, ux)), base);
-        const R feq = (WQ(q) * rho) * br;
+        // offset form: feq - w = (w rho) br - w
+        const R feq = OFS ? fma(WQ(q) * rho, br, splat(-WQ(q), ux)) : (WQ(q) * rho) * br;
         R fn = fma(splat(omega, ux), feq - f[q], f[q]);
         if (forced) {
             // w (1 - omega/2) [ (3(c - u) + 9 (c.u) c) . F ]
@@ -423,7 +453,7 @@ __device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R F
 // [rho, e, eps, jx, qx, jy, qy, pxx, pxy]; the equilibrium moments are
 // M f_eq of the second-order equilibrium in closed form; the back transform
 // uses M^-1 = M^T diag(1/|row|^2) (the rows are orthogonal).
-template <typename R>
+template <typename R, bool OFS = false>
 __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R Fy, const float S[9],
                                             bool force_quirk, bool forced) {
     const R axis = (f[1] + f[2]) + (f[3] + f[4]);
@@ -443,8 +473,12 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
     const R uu = fma(ux, ux, uy * uy);
     const R rux = rho * ux, ruy = rho * uy;
     R meq[9];
-    meq[1] = rho * fma(splat(3.0f, rho), uu, splat(-2.0f, rho));
-    meq[2] = rho * fma(splat(-3.0f, rho), uu, splat(1.0f, rho));
+    // offset form: m and a are taken relative to the moments of w, (1, -2, 1,
+    // 0, ...): meq[1], meq[2] and a[0] shift by constants, m[1..8] need none
+    meq[1] = OFS ? fma(rho, fma(splat(3.0f, rho), uu, splat(-2.0f, rho)), splat(2.0f, rho))
+                 : rho * fma(splat(3.0f, rho), uu, splat(-2.0f, rho));
+    meq[2] = OFS ? fma(rho, fma(splat(-3.0f, rho), uu, splat(1.0f, rho)), splat(-1.0f, rho))
+                 : rho * fma(splat(-3.0f, rho), uu, splat(1.0f, rho));
     meq[3] = rux;
     meq[4] = -rux;
     meq[5] = ruy;
@@ -456,7 +490,7 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
     const float inv_norm[9] = {1.0f / 9.0f, 1.0f / 36.0f, 1.0f / 36.0f, 1.0f / 6.0f, 1.0f / 12.0f,
                                1.0f / 6.0f, 1.0f / 12.0f, 0.25f, 0.25f};
     R a[9];
-    a[0] = (1.0f / 9.0f) * rho;
+    a[0] = OFS ? fma(splat(1.0f / 9.0f, rho), rho, splat(-1.0f / 9.0f, rho)) : (1.0f / 9.0f) * rho;
 #pragma unroll
     for (int k = 1; k < 9; k++) a[k] = inv_norm[k] * fma(splat(-S[k], rho), m[k] - meq[k], m[k]);
     if (forced) {
@@ -495,14 +529,16 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
 // or the adapter rate `hor` for i > 5 (NoAdapter: use_hor = false), back
 // transform through raw moments (binomial shift) and the raw-moment basis
 // of D2Q9, the same linear map as the reference's closed-form T^-1(u).
-template <typename R>
+template <typename R, bool OFS = false>
 __device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy, const float S[9], R hor,
                                            bool use_hor) {
     const R m10 = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const R m01 = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
-    const R m22 = (f[5] + f[6]) + (f[7] + f[8]);
-    const R m20 = (f[1] + f[3]) + m22;
-    const R m02 = (f[2] + f[4]) + m22;
+    // offset form: the raw moments of w are m20 = m02 = 1/3, m22 = 1/9
+    const R d22 = (f[5] + f[6]) + (f[7] + f[8]);
+    const R m22 = OFS ? d22 + splat(1.0f / 9.0f, rho) : d22;
+    const R m20 = (f[1] + f[3]) + (OFS ? d22 + splat(1.0f / 3.0f, rho) : d22);
+    const R m02 = (f[2] + f[4]) + (OFS ? d22 + splat(1.0f / 3.0f, rho) : d22);
     const R m11 = (f[5] + f[7]) - (f[6] + f[8]);
     const R m21 = (f[5] + f[6]) - (f[7] + f[8]);
     const R m12 = (f[5] + f[8]) - (f[6] + f[7]);
@@ -541,6 +577,7 @@ __device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy
     const R c20 = 0.5f * (t3 + t4), c02 = 0.5f * (t3 - t4);
     const R c00 = rho;
     // back to raw moments (binomial shift by +u), then to populations
+    // (offset form: minus the raw moments of w, 1, 1/3, 1/3, 1/9)
     const R r10 = fma(ux, c00, c10);
     const R r01 = fma(uy, c00, c01);
     const R r20 = fma(ux2, c00, fma(two * ux, c10, c20));
@@ -553,15 +590,19 @@ __device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy
                           fma(two * (ux * uy2), c10,
                               fma(splat(4.0f, rho) * uxy, c11,
                                   fma(uy2, c20, fma(ux2, c02, fma(two * uy, c21, fma(two * ux, c12, c22))))))));
-    f[0] = (c00 - (r20 + r02)) + r22;
-    f[1] = 0.5f * ((r10 + r20) - (r12 + r22));
-    f[3] = 0.5f * ((r20 + r12) - (r10 + r22));
-    f[2] = 0.5f * ((r01 + r02) - (r21 + r22));
-    f[4] = 0.5f * ((r02 + r21) - (r01 + r22));
-    f[5] = 0.25f * ((r11 + r21) + (r12 + r22));
-    f[6] = 0.25f * ((r21 + r22) - (r11 + r12));
-    f[7] = 0.25f * ((r11 + r22) - (r21 + r12));
-    f[8] = 0.25f * ((r12 + r22) - (r11 + r21));
+    const R o00 = OFS ? c00 - splat(1.0f, rho) : c00;
+    const R o20 = OFS ? r20 - splat(1.0f / 3.0f, rho) : r20;
+    const R o02 = OFS ? r02 - splat(1.0f / 3.0f, rho) : r02;
+    const R o22 = OFS ? r22 - splat(1.0f / 9.0f, rho) : r22;
+    f[0] = (o00 - (o20 + o02)) + o22;
+    f[1] = 0.5f * ((r10 + o20) - (r12 + o22));
+    f[3] = 0.5f * ((o20 + r12) - (r10 + o22));
+    f[2] = 0.5f * ((r01 + o02) - (r21 + o22));
+    f[4] = 0.5f * ((o02 + r21) - (r01 + o22));
+    f[5] = 0.25f * ((r11 + r21) + (r12 + o22));
+    f[6] = 0.25f * ((r21 + o22) - (r11 + r12));
+    f[7] = 0.25f * ((r11 + o22) - (r21 + r12));
+    f[8] = 0.25f * ((r12 + o22) - (r11 + r21));
 }
 
 // OptimalAdapter::compute_higher_order_relaxation -- adapters.cuh:48-111

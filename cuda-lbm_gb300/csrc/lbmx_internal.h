@@ -130,6 +130,7 @@ cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w
 // kernel also runs 64 x 8 and 128 x 8 tiles.
 constexpr int kStepThreads = 288;  // 8 consumer warps + 1 producer warp
 constexpr int kConsumerWarps = 8;
+constexpr int kCtasPerSm = 3;      // resident persistent CTAs per SM (72 registers per thread)
 constexpr int kStageW = 128;
 constexpr int kStageH = 4;
 constexpr int kSpecialChunk = kConsumerWarps * 32;  // special nodes per work item (one per consumer thread)

@@ -227,25 +227,39 @@ struct Staging {
     static constexpr int STAGE_ELEMS = 9 * SLAB;
     static constexpr unsigned STAGE_BYTES = (unsigned)(9 * BOX_ELEMS * sizeof(T));  // bytes the nine boxes bring
     static constexpr size_t BUF_BYTES = (size_t)NST * STAGE_ELEMS * sizeof(T);
-    // after the buffers: full[NST], empty[NST] mbarriers, tile id per stage
-    static constexpr size_t SMEM = BUF_BYTES + 2 * NST * sizeof(uint64_t) + NST * sizeof(int);
+    // after the buffers: full[NST], empty[NST] mbarriers, one work slot per stage
+    static constexpr size_t SMEM = BUF_BYTES + 2 * NST * sizeof(uint64_t) + NST * sizeof(int4);
 };
 
 constexpr unsigned kWaitLimit = 1u << 20;  // polls before a wait gives up
+
+// Work slot of a stage, written by the producer before it arms the stage's
+// full barrier and read by the consumers after the barrier completes:
+// code >= 0 an interior tile whose first node is (x0, y0); code <= -2 special
+// chunk -code - 2; code == -1 no more work.  w: the lattice (batched kernel).
+__device__ __forceinline__ void put_slot(int4* slot, int code, int x0, int y0, int w) {
+    volatile int* p = reinterpret_cast<volatile int*>(slot);
+    p[0] = code;
+    p[1] = x0;
+    p[2] = y0;
+    p[3] = w;
+}
+__device__ __forceinline__ int4 get_slot(const int4* slot) {
+    const volatile int* p = reinterpret_cast<const volatile int*>(slot);
+    return make_int4(p[0], p[1], p[2], p[3]);
+}
 
 // Issue the nine box loads of one tile into stage buffer `buf` (producer warp;
 // lane 0 has already armed `bar` with Staging<T>::STAGE_BYTES).  Population q
 // lands in slab q (TH rows of TWP elements); node x of tile row r then sits at
 // column x - x0 + A - (parity-1 x shift of q).
 template <typename T, int P, int TW = kStageW, int TH = kStageH>
-__device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap* tmap, int tile, T* buf,
+__device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap* tmap, int x0, int y0, T* buf,
                                             uint64_t* bar) {
     using St = Staging<T, TW, TH>;
     const int lane = threadIdx.x & 31;
     if (lane >= 9) return;
     const int q = lane;
-    const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
-    const int x0 = tx * St::TW, y0 = 1 + ty * St::TH;
     // parity 1 reads slot OPP(q) of the upstream nodes, rows shifted by -c_y(q)
     int plane, dy;
     switch (q) {
@@ -271,15 +285,19 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     const long long off = (long long)y * g.pitch + x0;
     const long long plane = g.plane;
     const int pitch = g.pitch;
+    // 16-bit storage: f holds the stored offsets f - w throughout (the
+    // collision works in offset form); FP32: f itself
+    constexpr bool OFS = kOffset<T>;
     V2 f[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) {
         const bool shifted = P && CX(q) != 0;
         const T* s = sbuf + q * St::SLAB + r * St::TWP + 2 * lx + (shifted ? St::A - CX(q) : St::A);
-        if (shifted) f[q].v = make_float2(Store<T>::ld(s, WQ(q)), Store<T>::ld(s + 1, WQ(q)));
-        else f[q].v = Store<T>::ld2(s, WQ(q));
+        if (shifted) f[q].v = make_float2(Store<T>::ldr(s), Store<T>::ldr(s + 1));
+        else f[q].v = Store<T>::ld2r(s);
     }
-    const V2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    V2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    if (OFS) rho = rho + splat(1.0f, rho);  // the weights sum to 1
     const V2 jx = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const V2 jy = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
     V2 Fx = {make_float2(a.body_fx, a.body_fx)}, Fy = {make_float2(a.body_fy, a.body_fy)};
@@ -292,7 +310,8 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     const V2 uy = fma(0.5f * Fy, inv, jy * inv);
     V2 pimag = splat(0.f, rho);
     if (OP == LBMX_CM_OPT || a.partials) {
-        const V2 d = (f[5] + f[6]) + (f[7] + f[8]);
+        // offset form: sum c_x^2 w = sum c_y^2 w = 1/3
+        const V2 d = OFS ? (f[5] + f[6]) + ((f[7] + f[8]) + splat(1.0f / 3.0f, rho)) : (f[5] + f[6]) + (f[7] + f[8]);
         const V2 pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
         const V2 pxy = (f[5] + f[7]) - (f[6] + f[8]);
         pimag = vsqrt(fma(pxx, pxx, fma(2.0f * pxy, pxy, pyy * pyy)));
@@ -312,28 +331,28 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     }
     if (a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {
-        collide_bgk<V2>(f, rho, ux, uy, Fx, Fy, a.omega, a.forced);
+        collide_bgk<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.omega, a.forced);
     } else if (OP == LBMX_MRT) {
-        collide_mrt<V2>(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
+        collide_mrt<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
     } else if (OP == LBMX_CM) {
-        collide_cm<V2>(f, rho, ux, uy, Fx, Fy, a.S, rho, false);
+        collide_cm<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.S, rho, false);
     } else {
         const V2 jmag = rho * vsqrt(fma(ux, ux, uy * uy));
-        collide_cm<V2>(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate<V2>(rho, jmag, pimag, a.avg), true);
+        collide_cm<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate<V2>(rho, jmag, pimag, a.avg), true);
     }
-    Store<T>::st2(F + a.rest_plane * plane + off, f[0].v, WQ(0));
+    Store<T>::st2r(F + a.rest_plane * plane + off, f[0].v);
 #pragma unroll
     for (int q = 1; q < 9; q++) {
         if (P == 0) {
-            Store<T>::st2(F + OPP(q) * plane + off, f[q].v, WQ(q));  // own slot OPP(q)
+            Store<T>::st2r(F + OPP(q) * plane + off, f[q].v);  // own slot OPP(q)
         } else {
             // slot q of the downstream nodes x + c_q
             T* p = F + q * plane + off + (long long)CY(q) * pitch + CX(q);
             if (CX(q) == 0) {
-                Store<T>::st2(p, f[q].v, WQ(q));
+                Store<T>::st2r(p, f[q].v);
             } else {
-                Store<T>::st(p, f[q].v.x, WQ(q));
-                Store<T>::st(p + 1, f[q].v.y, WQ(q));
+                Store<T>::str(p, f[q].v.x);
+                Store<T>::str(p + 1, f[q].v.y);
             }
         }
     }
@@ -351,7 +370,7 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
 }
 
 template <typename T, int OP, int P>
-__global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
     // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
     // work item from a global counter; for an interior tile it bulk-copies
     // the tile into the ring), warps 0-7 consume.  Items 0..special_chunks-1
@@ -367,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, con
     T* bufs = reinterpret_cast<T*>(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + St::BUF_BYTES);
     uint64_t* empty = full + St::NST;
-    volatile int* item_id = reinterpret_cast<volatile int*>(empty + St::NST);
+    int4* slot = reinterpret_cast<int4*>(empty + St::NST);
     const int nchunks = a.special_chunks;
     const int nitems = nchunks + a.tiles_x * a.tiles_y;
     const int warp = tid >> 5, lane = tid & 31;
@@ -401,26 +420,29 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, con
             left--;
             if (item >= nitems) {
                 if (lane == 0) {
-                    item_id[s] = -1;
+                    put_slot(&slot[s], -1, 0, 0, 0);
                     mbar_arrive(&full[s]);
                 }
                 break;
             }
             if (item < nchunks) {
                 if (lane == 0) {
-                    item_id[s] = item;
+                    put_slot(&slot[s], -2 - item, 0, 0, 0);
                     mbar_arrive(&full[s]);
                 }
                 __syncwarp();
                 continue;
             }
+            const int tile = item - nchunks;
+            const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
+            const int x0 = tx * St::TW, y0 = 1 + ty * St::TH;
             if (lane == 0) {
-                item_id[s] = item;
+                put_slot(&slot[s], tile, x0, y0, 0);
                 fence_proxy_async_smem();
                 mbar_expect_tx(&full[s], St::STAGE_BYTES);
             }
             __syncwarp();
-            stage_issue<T, P>(a, &tmap, item - nchunks, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+            stage_issue<T, P>(a, &tmap, x0, y0, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
         }
         // On the normal path the consumers have waited for every fill.  If
         // they stopped releasing stages, let the fills still unconsumed
@@ -437,14 +459,12 @@ __global__ void __launch_bounds__(kThreads, 2) step_kernel(const StepArgs a, con
                 if (lane == 0) atomicOr(a.error_word, 2u);
                 break;
             }
-            const int item = item_id[s];
-            if (item < 0) break;
-            if (item < nchunks) {
-                special_chunk<T, OP>(a, item, tid, v);
+            const int4 sl = get_slot(&slot[s]);
+            if (sl.x == -1) break;
+            if (sl.x < 0) {
+                special_chunk<T, OP>(a, -2 - sl.x, tid, v);
             } else {
-                const int tile = item - nchunks;
-                const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
-                const int x0 = tx * St::TW + 2 * lx, y = 1 + ty * St::TH + r;
+                const int x0 = sl.y + 2 * lx, y = sl.z + r;
                 bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
                 if (live && a.special_bits) {
                     const long long unit = ((long long)y * a.g.pitch + x0) >> 1;

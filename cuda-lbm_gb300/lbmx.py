@@ -281,7 +281,7 @@ class Batch:
         self._check(self.lib.lbmx_batch_get_config(self.b, ctypes.byref(c)))
         return c.as_dict()
 
-    def set_config(self, tile_w=128, tile_h=4, ctas_per_sm=2, chunk=1, graph_steps=16):
+    def set_config(self, tile_w=128, tile_h=4, ctas_per_sm=3, chunk=1, graph_steps=16):
         c = BatchConfig(tile_w, tile_h, ctas_per_sm, chunk, graph_steps)
         self._check(self.lib.lbmx_batch_set_config(self.b, ctypes.byref(c)))
 

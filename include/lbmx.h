@@ -240,7 +240,7 @@ typedef struct lbmx_batch lbmx_batch;
 typedef struct lbmx_batch_config {
     int32_t tile_w;       /* interior tile shape tile_w x tile_h: 64 x 8, 128 x 4 or 128 x 8 */
     int32_t tile_h;
-    int32_t ctas_per_sm;  /* persistent CTAs per SM: 1 or 2 */
+    int32_t ctas_per_sm;  /* persistent CTAs per SM: 1, 2 or 3 */
     int32_t chunk;        /* work items claimed per atomic: 1..64 */
     int32_t graph_steps;  /* steps per CUDA graph replay: 0 (no graph) or even, <= 64 */
 } lbmx_batch_config;
