@@ -1,0 +1,802 @@
+// lbmx_adjoint.cu -- discrete adjoint of the D2Q9 step (no reference
+// counterpart): gradients of an objective built from the step's moments with
+// respect to the per-node Brinkman field gamma, the relaxation rate omega and
+// the body force, by checkpointed recomputation.
+//
+// Forward model (the engine's step, written densely with ping-pong buffers):
+//   ps_t[x][q] = pc_{t-1}[x - c_q][q]          streaming (periodic wrap);
+//                pc_{t-1}[x][OPP q] - W(OPP q)  half-way wall node, link out
+//   fb_t = B(ps_t)                             on-node bounce-back (flag 1)
+//   (pc_t, rho_t, u_t) = N(fb_t; gamma, omega, F [, averages_t])
+//   J = sum over t >= first, x of w_rho rho + w_x rho u_x + w_y rho u_y
+// N is the engine's per-node code: macroscopics, Guo force correction,
+// Brinkman drag, collision (BGK, MRT, CM, CM_OPT).
+//
+// Reverse step t, per node x:
+//   mu[q]  = lambda_{t+1}[x + c_q][q]  (the half-way reflection for links
+//            that leave a wall node; 0 for links that leave the domain)
+//   lambda_t[x][i] = sum_q mu[q] dpc_q/dps_i + sum_m w_m dmoment_m/dps_i
+// with the Jacobian columns from forward-mode tangents (lbmx_dual.cuh)
+// through B and N -- the same templated device code as the forward step --
+// and the parameter gradients from the tangents of gamma, omega and F.
+// CM_OPT's rate depends on grid averages of the step; their sensitivity is
+// reduced over the grid and returned to every node in a second pass.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "lbmx_dual.cuh"
+
+namespace lbmx {
+namespace {
+
+constexpr int kAdjBlock = 256;
+constexpr int kTan = 2;  // tangents per pass
+
+struct AdjGeom {
+    int nx, ny, px, py;
+    long long n;
+};
+
+struct AdjArgs {
+    AdjGeom g;
+    uint32_t quirks;
+    float omega;
+    float S[9];
+    uint32_t omega_mask;  // S entries tied to omega (their common value is the omega of the gradient)
+    float fx, fy;         // uniform body force
+    float wall_ux, wall_uy;
+    const uint8_t* flags;   // [n] or null
+    const float* gamma;     // [n] or null
+    const float* weights;   // [3][n] objective weights or null
+};
+
+__device__ __forceinline__ bool adj_halfway(uint8_t fl) { return fl == LBMX_MOVING_WALL_BB || fl == LBMX_HALFWAY_BB; }
+
+__device__ __forceinline__ float adj_wall_term(const AdjArgs& a, int q, uint8_t fl) {
+    if (fl != LBMX_MOVING_WALL_BB) return 0.0f;
+    return 6.0f * WQ(q) * ((float)CX(q) * a.wall_ux + (float)CY(q) * a.wall_uy);
+}
+
+// node x + s * c_q (wrapped on periodic axes), or -1 outside the domain
+__device__ __forceinline__ long long adj_link(const AdjGeom& g, int x, int y, int q, int s) {
+    int nx = x + s * CX(q), ny = y + s * CY(q);
+    if (nx < 0 || nx >= g.nx) {
+        if (!g.px) return -1;
+        nx = nx < 0 ? nx + g.nx : nx - g.nx;
+    }
+    if (ny < 0 || ny >= g.ny) {
+        if (!g.py) return -1;
+        ny = ny < 0 ? ny + g.ny : ny - g.ny;
+    }
+    return (long long)ny * g.nx + nx;
+}
+
+// post-stream populations of node (x, y) from the previous post-collision state
+__device__ __forceinline__ void adj_gather(const AdjArgs& a, const float* pc, int x, int y, long long node, uint8_t fl,
+                                           float ps[9]) {
+    const long long n = a.g.n;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        const long long s = adj_link(a.g, x, y, q, -1);
+        if (s >= 0) ps[q] = pc[q * n + s];
+        else if (adj_halfway(fl)) ps[q] = pc[OPP(q) * n + node] - adj_wall_term(a, OPP(q), fl);
+        else ps[q] = 0.0f;  // overwritten by the node's bounce-back (checked on the host)
+    }
+}
+
+// BounceBack<2>::apply as the engine applies it (the domain edge, whatever
+// the periodicity, bbDomainBoundary.cuh:26-49)
+template <typename R>
+__device__ __forceinline__ void adj_bc(const AdjGeom& g, R f[9], int x, int y, uint8_t fl) {
+    if (fl != LBMX_BOUNCE_BACK) return;
+#pragma unroll
+    for (int i = 1; i < 9; i++) {
+        const int xn = x + CX(i), yn = y + CY(i);
+        if (xn < 0 || xn >= g.nx || yn < 0 || yn >= g.ny) f[OPP(i)] = f[i];
+    }
+}
+
+// density and force-corrected, Brinkman-corrected velocity, as general_node
+template <typename R>
+__device__ __forceinline__ void adj_macro(const R f[9], R gm, R& Fx, R& Fy, R& rho, R& ux, R& uy) {
+    rho = f[0];
+    R jx = splat(0.0f, f[0]), jy = splat(0.0f, f[0]);
+#pragma unroll
+    for (int q = 1; q < 9; q++) {
+        rho = rho + f[q];
+        if (CX(q) == 1) jx = jx + f[q];
+        if (CX(q) == -1) jx = jx - f[q];
+        if (CY(q) == 1) jy = jy + f[q];
+        if (CY(q) == -1) jy = jy - f[q];
+    }
+    const R inv = vdiv(splat(1.0f, rho), rho);
+    ux = jx * inv + vdiv(0.5f * Fx, rho);
+    uy = jy * inv + vdiv(0.5f * Fy, rho);
+    brinkman<R>(gm, rho, ux, uy, Fx, Fy);
+}
+
+template <typename R>
+__device__ __forceinline__ R adj_pimag(const R f[9]) {
+    const R d = ((f[5] + f[6]) + f[7]) + f[8];
+    const R pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
+    const R pxy = ((f[5] - f[6]) + f[7]) - f[8];
+    return vsqrt(fma(pxx, pxx, fma(2.0f * pxy, pxy, pyy * pyy)));
+}
+
+// N: f (post-boundary) -> post-collision; mom = (rho, ux, uy)
+template <typename R, int OP>
+__device__ __forceinline__ void adj_node(const AdjArgs& a, R f[9], R gm, R Fx, R Fy, R omega, const R S[9],
+                                         const R avg[3], R mom[3]) {
+    R rho, ux, uy;
+    adj_macro<R>(f, gm, Fx, Fy, rho, ux, uy);
+    mom[0] = rho;
+    mom[1] = ux;
+    mom[2] = uy;
+    if (OP == LBMX_BGK) {
+        collide_bgk<R, false, R>(f, rho, ux, uy, Fx, Fy, omega, true);
+    } else if (OP == LBMX_MRT) {
+        collide_mrt<R, false, R>(f, rho, ux, uy, Fx, Fy, S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, true);
+    } else if (OP == LBMX_CM) {
+        collide_cm<R, false, R>(f, rho, ux, uy, Fx, Fy, S, rho, false);
+    } else {
+        const R pimag = adj_pimag<R>(f);
+        const R jmag = vsqrt(fma(ux, ux, uy * uy)) * rho;
+        collide_cm<R, false, R>(f, rho, ux, uy, Fx, Fy, S, optimal_rate<R, R>(rho, jmag, pimag, avg), true);
+    }
+}
+
+// the node's terms of the CM_OPT grid averages: rho, rho |u|, |Pi|
+template <typename R>
+__device__ __forceinline__ void adj_avg_terms(const R f[9], R gm, R Fx, R Fy, R out[3]) {
+    R rho, ux, uy;
+    adj_macro<R>(f, gm, Fx, Fy, rho, ux, uy);
+    out[0] = rho;
+    out[1] = rho * vsqrt(fma(ux, ux, uy * uy));
+    out[2] = adj_pimag<R>(f);
+}
+
+// deterministic block sums of C values; part[block][C] = (or +=) the sum
+template <int C>
+__device__ __forceinline__ void adj_block_sum(double v[C], double* part, bool add) {
+    __shared__ double sh[kAdjBlock / 32][C];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        double t = v[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[warp][c] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < C; c++) {
+            double s = 0.0;
+            for (int w = 0; w < kAdjBlock / 32; w++) s += sh[w][c];
+            if (add) part[(long long)blockIdx.x * C + c] += s;
+            else part[(long long)blockIdx.x * C + c] = s;
+        }
+    }
+}
+
+__global__ void adj_init_kernel(AdjGeom g, const float* rho, const float* u, float* pc) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    float fe[9];
+    init_equilibrium(rho[i], u[i], u[g.n + i], fe);
+#pragma unroll
+    for (int q = 0; q < 9; q++) pc[q * g.n + i] = fe[q];
+}
+
+// grid averages of step t (CM_OPT), block sums
+__global__ void adj_avg_kernel(const AdjArgs a, const float* pc_prev, double* part) {
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (node < a.g.n) {
+        const int y = (int)(node / a.g.nx), x = (int)(node - (long long)y * a.g.nx);
+        const uint8_t fl = a.flags ? a.flags[node] : (uint8_t)0;
+        float f[9];
+        adj_gather(a, pc_prev, x, y, node, fl, f);
+        adj_bc<float>(a.g, f, x, y, fl);
+        float t[3];
+        adj_avg_terms<float>(f, a.gamma ? a.gamma[node] : 0.0f, a.fx, a.fy, t);
+        v[0] = t[0];
+        v[1] = t[1];
+        v[2] = t[2];
+    }
+    adj_block_sum<3>(v, part, false);
+}
+
+// one step forward; the objective terms accumulate per node when `objective`
+template <int OP>
+__global__ void adj_forward_kernel(const AdjArgs a, const float* pc_prev, float* pc_next, const float* avg,
+                                   int objective, double* jnode, float* rho_out, float* u_out) {
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= a.g.n) return;
+    const long long n = a.g.n;
+    const int y = (int)(node / a.g.nx), x = (int)(node - (long long)y * a.g.nx);
+    const uint8_t fl = a.flags ? a.flags[node] : (uint8_t)0;
+    float f[9];
+    adj_gather(a, pc_prev, x, y, node, fl, f);
+    adj_bc<float>(a.g, f, x, y, fl);
+    float mom[3];
+    const float av[3] = {avg ? avg[0] : 1.0f, avg ? avg[1] : 1.0f, avg ? avg[2] : 1.0f};
+    adj_node<float, OP>(a, f, a.gamma ? a.gamma[node] : 0.0f, a.fx, a.fy, a.omega, a.S, av, mom);
+#pragma unroll
+    for (int q = 0; q < 9; q++) pc_next[q * n + node] = f[q];
+    if (objective && a.weights)
+        jnode[node] += (double)a.weights[node] * mom[0] + (double)a.weights[n + node] * (mom[0] * mom[1]) +
+                       (double)a.weights[2 * n + node] * (mom[0] * mom[2]);
+    if (rho_out) {
+        rho_out[node] = mom[0];
+        u_out[node] = mom[1];
+        u_out[n + node] = mom[2];
+    }
+}
+
+// Reverse of step t.  lam_next = lambda_{t+1} (null at the last step);
+// writes lambda_t; g_gamma[node] += dJ/dgamma; part[block] += (domega, dFx,
+// dFy); CM_OPT: avg_part[block] = this step's sensitivity to the averages.
+template <int OP>
+__global__ void __launch_bounds__(kAdjBlock) adj_reverse_kernel(const AdjArgs a, const float* pc_prev,
+                                                                const float* lam_next, float* lam_out,
+                                                                const float* avg, int objective, double* g_gamma,
+                                                                double* part, double* avg_part) {
+    constexpr int D = OP == LBMX_CM_OPT ? 16 : 13;  // ps[9], gamma, omega, Fx, Fy [, averages]
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double sums[3] = {0.0, 0.0, 0.0}, asums[3] = {0.0, 0.0, 0.0};
+    if (node < a.g.n) {
+        const long long n = a.g.n;
+        const int y = (int)(node / a.g.nx), x = (int)(node - (long long)y * a.g.nx);
+        const uint8_t fl = a.flags ? a.flags[node] : (uint8_t)0;
+        float mu[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            float m = 0.0f;
+            if (lam_next) {
+                const long long d = adj_link(a.g, x, y, q, 1);
+                if (d >= 0) m = lam_next[q * n + d];
+                else if (adj_halfway(fl)) m = lam_next[OPP(q) * n + node];
+            }
+            mu[q] = m;
+        }
+        float ps[9];
+        adj_gather(a, pc_prev, x, y, node, fl, ps);
+        float w[3] = {0.0f, 0.0f, 0.0f};
+        if (objective && a.weights) {
+            w[0] = a.weights[node];
+            w[1] = a.weights[n + node];
+            w[2] = a.weights[2 * n + node];
+        }
+        const float gm = a.gamma ? a.gamma[node] : 0.0f;
+        float s[D];
+        using R = Dual<kTan>;
+#pragma unroll 1
+        for (int p0 = 0; p0 < D; p0 += kTan) {
+            R f[9], S[9], av[3], mom[3];
+            auto seed = [&](float v, int dir) {
+                R r = dconst<kTan>(v);
+#pragma unroll
+                for (int k = 0; k < kTan; k++) r.d[k] = (p0 + k == dir) ? 1.0f : 0.0f;
+                return r;
+            };
+#pragma unroll
+            for (int q = 0; q < 9; q++) f[q] = seed(ps[q], q);
+            const R g = seed(gm, 9);
+            const R om = seed(a.omega, 10);
+#pragma unroll
+            for (int k = 0; k < 9; k++) S[k] = seed(a.S[k], ((a.omega_mask >> k) & 1u) ? 10 : -1);
+            const R Fx = seed(a.fx, 11), Fy = seed(a.fy, 12);
+#pragma unroll
+            for (int j = 0; j < 3; j++) av[j] = seed(avg ? avg[j] : 1.0f, 13 + j);
+            adj_bc<R>(a.g, f, x, y, fl);
+            adj_node<R, OP>(a, f, g, Fx, Fy, om, S, av, mom);
+            const R jx = mom[0] * mom[1], jy = mom[0] * mom[2];
+#pragma unroll
+            for (int k = 0; k < kTan; k++) {
+                if (p0 + k >= D) break;
+                float t = w[0] * mom[0].d[k] + w[1] * jx.d[k] + w[2] * jy.d[k];
+#pragma unroll
+                for (int q = 0; q < 9; q++) t = fmaf(mu[q], f[q].d[k], t);
+                s[p0 + k] = t;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 9; q++) lam_out[q * n + node] = s[q];
+        g_gamma[node] += s[9];
+        sums[0] = s[10];
+        sums[1] = s[11];
+        sums[2] = s[12];
+        if (OP == LBMX_CM_OPT) {
+            asums[0] = s[13 % D];
+            asums[1] = s[14 % D];
+            asums[2] = s[15 % D];
+        }
+    }
+    adj_block_sum<3>(sums, part, true);
+    if (OP == LBMX_CM_OPT) {
+        __syncthreads();
+        adj_block_sum<3>(asums, avg_part, false);
+    }
+}
+
+// CM_OPT: lambda_t += (1/N) G . d(terms)/dps with G the reduced sensitivity
+__global__ void adj_avg_back_kernel(const AdjArgs a, const float* pc_prev, const double* G, float* lam_out) {
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= a.g.n) return;
+    const long long n = a.g.n;
+    const int y = (int)(node / a.g.nx), x = (int)(node - (long long)y * a.g.nx);
+    const uint8_t fl = a.flags ? a.flags[node] : (uint8_t)0;
+    float ps[9];
+    adj_gather(a, pc_prev, x, y, node, fl, ps);
+    const float inv_n = (float)(1.0 / (double)n);
+    const float g0 = (float)G[0] * inv_n, g1 = (float)G[1] * inv_n, g2 = (float)G[2] * inv_n;
+    const float gm = a.gamma ? a.gamma[node] : 0.0f;
+    using R = Dual<kTan>;
+#pragma unroll 1
+    for (int p0 = 0; p0 < 9; p0 += kTan) {
+        R f[9], t[3];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            f[q] = dconst<kTan>(ps[q]);
+#pragma unroll
+            for (int k = 0; k < kTan; k++) f[q].d[k] = (p0 + k == q) ? 1.0f : 0.0f;
+        }
+        adj_bc<R>(a.g, f, x, y, fl);
+        adj_avg_terms<R>(f, dconst<kTan>(gm), dconst<kTan>(a.fx), dconst<kTan>(a.fy), t);
+#pragma unroll
+        for (int k = 0; k < kTan; k++) {
+            const int q = p0 + k;
+            if (q >= 9) break;
+            lam_out[q * n + node] += g0 * t[0].d[k] + g1 * t[1].d[k] + g2 * t[2].d[k];
+        }
+    }
+}
+
+// out[c] = sum over `count` rows of part[row][c] (one block, fixed order)
+__global__ void adj_sum_kernel(const double* part, long long count, int C, double* out, int add) {
+    __shared__ double sh[kAdjBlock];
+    for (int c = 0; c < C; c++) {
+        double t = 0.0;
+        for (long long r = threadIdx.x; r < count; r += kAdjBlock) t += part[r * C + c];
+        sh[threadIdx.x] = t;
+        __syncthreads();
+        for (int s = kAdjBlock / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[c] = add ? out[c] + sh[0] : sh[0];
+        __syncthreads();
+    }
+}
+
+__global__ void adj_mean_kernel(const double* s, float* out, double inv) {
+    // float means, as the engine's pre-pass stores them
+    out[0] = (float)(s[0] * inv);
+    out[1] = (float)(s[1] * inv);
+    out[2] = (float)(s[2] * inv);
+}
+
+__global__ void adj_to_float_kernel(const double* src, float* dst, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+}  // namespace
+}  // namespace lbmx
+
+using namespace lbmx;
+
+struct lbmx_adjoint {
+    lbmx_params p;
+    AdjArgs args;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long n = 0;
+    int every = 1;          // checkpoint interval
+    int T = 0;              // steps of the last forward run
+    int first = 1;          // objective sums steps first..T
+    uint8_t* flags = nullptr;
+    float* gamma = nullptr;
+    float* weights = nullptr;
+    float* pc0 = nullptr;   // initial post-collision state [9][n]
+    float* ping[2] = {nullptr, nullptr};
+    float* ckpt = nullptr;  // [ncheck][9][n]
+    int ncheck_cap = 0;
+    float* seg = nullptr;   // [every + 1][9][n]
+    float* lam[2] = {nullptr, nullptr};
+    float* avg_hist = nullptr;  // [T + 1][3]
+    int avg_cap = 0;
+    double* jnode = nullptr;
+    double* g_gamma = nullptr;
+    double* part = nullptr;     // [blocks][3]
+    double* avg_part = nullptr; // [blocks][3]
+    double* red = nullptr;      // [8] reductions
+    float* rho_out = nullptr;
+    float* u_out = nullptr;
+    long long blocks = 0;
+    bool have_state = false, have_forward = false;
+    char err[512] = {0};
+};
+
+static char g_adj_err[512];
+
+static lbmx_status afail(lbmx_adjoint* a, lbmx_status code, const char* fmt, ...) {
+    char* dst = a ? a->err : g_adj_err;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(dst, 512, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define ADJ_CUDA(a, call)                                                                            \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return afail((a), e_ == cudaErrorMemoryAllocation ? LBMX_ERR_OUT_OF_MEMORY : LBMX_ERR_CUDA, \
+                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);        \
+    } while (0)
+
+static void tie_omega(lbmx_adjoint* a) {
+    // the S entries equal to omega move with it
+    a->args.omega_mask = 0;
+    for (int k = 0; k < 9; k++)
+        if (a->p.op != LBMX_BGK && a->args.S[k] == a->args.omega) a->args.omega_mask |= 1u << k;
+}
+
+// Flags the adjoint can differentiate, and every population a bounce-back
+// node reads from outside the domain overwritten from inside it.
+static lbmx_status check_flags(lbmx_adjoint* a, const std::vector<uint8_t>& fl) {
+    const int nx = a->p.nx, ny = a->p.ny;
+    const bool px = a->p.periodic_x, py = a->p.periodic_y;
+    auto outside = [&](int x, int y, bool periodic_aware) {
+        const bool ox = x < 0 || x >= nx, oy = y < 0 || y >= ny;
+        return periodic_aware ? ((ox && !px) || (oy && !py)) : (ox || oy);
+    };
+    for (int y = 0; y < ny; y++)
+        for (int x = 0; x < nx; x++) {
+            const uint8_t f = fl[(size_t)y * nx + x];
+            if (f != LBMX_FLUID && f != LBMX_BOUNCE_BACK && f != LBMX_HALFWAY_BB && f != LBMX_MOVING_WALL_BB)
+                return afail(a, LBMX_ERR_UNSUPPORTED,
+                             "lbmx_adjoint: flag %d at (%d,%d) is not differentiated (fluid, bounce-back and half-way "
+                             "walls are)", f, x, y);
+            bool known[9];
+            bool any_out = false;
+            for (int q = 0; q < 9; q++) {
+                known[q] = !outside(x - CX(q), y - CY(q), true);
+                any_out |= !known[q];
+            }
+            if (!any_out || f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB) continue;
+            if (f == LBMX_FLUID)
+                return afail(a, LBMX_ERR_UNSUPPORTED,
+                             "lbmx_adjoint: fluid node (%d,%d) on a non-periodic edge reads undefined populations", x, y);
+            for (int i = 1; i < 9; i++)
+                if (outside(x + CX(i), y + CY(i), false)) known[OPP(i)] = known[i];
+            for (int q = 0; q < 9; q++)
+                if (!known[q])
+                    return afail(a, LBMX_ERR_UNSUPPORTED,
+                                 "lbmx_adjoint: bounce-back node (%d,%d) keeps a population from outside the domain "
+                                 "(use half-way walls there)", x, y);
+        }
+    return LBMX_OK;
+}
+
+template <typename Fn>
+static cudaError_t op_dispatch(int op, Fn fn) {
+    switch (op) {
+    case LBMX_BGK: return fn(std::integral_constant<int, LBMX_BGK>());
+    case LBMX_MRT: return fn(std::integral_constant<int, LBMX_MRT>());
+    case LBMX_CM: return fn(std::integral_constant<int, LBMX_CM>());
+    default: return fn(std::integral_constant<int, LBMX_CM_OPT>());
+    }
+}
+
+static unsigned grid_of(long long n) { return (unsigned)((n + kAdjBlock - 1) / kAdjBlock); }
+
+// averages of step t (CM_OPT) into avg_hist[t]
+static lbmx_status step_averages(lbmx_adjoint* a, const float* pc_prev, int t) {
+    adj_avg_kernel<<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(a->args, pc_prev, a->avg_part);
+    ADJ_CUDA(a, cudaGetLastError());
+    adj_sum_kernel<<<1, kAdjBlock, 0, a->stream>>>(a->avg_part, a->blocks, 3, a->red, 0);
+    ADJ_CUDA(a, cudaGetLastError());
+    adj_mean_kernel<<<1, 1, 0, a->stream>>>(a->red, a->avg_hist + (size_t)3 * t, 1.0 / (double)a->n);
+    ADJ_CUDA(a, cudaGetLastError());
+    return LBMX_OK;
+}
+
+static lbmx_status forward_step(lbmx_adjoint* a, const float* prev, float* next, int t, bool objective,
+                                bool store) {
+    const bool opt = a->p.op == LBMX_CM_OPT;
+    if (opt) {
+        lbmx_status st = step_averages(a, prev, t);
+        if (st != LBMX_OK) return st;
+    }
+    const float* avg = opt ? a->avg_hist + (size_t)3 * t : nullptr;
+    ADJ_CUDA(a, op_dispatch(a->p.op, [&](auto opc) {
+                 adj_forward_kernel<decltype(opc)::value><<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(
+                     a->args, prev, next, avg, objective ? 1 : 0, a->jnode, store ? a->rho_out : nullptr,
+                     store ? a->u_out : nullptr);
+                 return cudaGetLastError();
+             }));
+    return LBMX_OK;
+}
+
+extern "C" {
+
+void lbmx_adjoint_destroy(lbmx_adjoint* a) {
+    if (!a) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(a->p.device);
+    if (a->stream) cudaStreamSynchronize(a->stream);
+    cudaFree(a->flags); cudaFree(a->gamma); cudaFree(a->weights); cudaFree(a->pc0);
+    cudaFree(a->ping[0]); cudaFree(a->ping[1]); cudaFree(a->ckpt); cudaFree(a->seg);
+    cudaFree(a->lam[0]); cudaFree(a->lam[1]); cudaFree(a->avg_hist); cudaFree(a->jnode);
+    cudaFree(a->g_gamma); cudaFree(a->part); cudaFree(a->avg_part); cudaFree(a->red);
+    cudaFree(a->rho_out); cudaFree(a->u_out);
+    if (a->own_stream && a->stream) cudaStreamDestroy(a->stream);
+    cudaSetDevice(cur);
+    delete a;
+}
+
+lbmx_status lbmx_adjoint_create(const lbmx_params* p, const uint8_t* flags, int32_t checkpoint_every,
+                                lbmx_adjoint** out) {
+    if (!out) return afail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_create: out is NULL");
+    *out = nullptr;
+    if (!p) return afail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_create: params is NULL");
+    if (p->nx < 3 || p->ny < 3 || (long long)p->nx * p->ny > (1LL << 31) - 1)
+        return afail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_create: bad lattice %d x %d", p->nx, p->ny);
+    if (p->op < LBMX_BGK || p->op > LBMX_CM_OPT)
+        return afail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_create: unknown operator %d", p->op);
+    if (p->storage != LBMX_STORAGE_F32)
+        return afail(nullptr, LBMX_ERR_UNSUPPORTED, "lbmx_adjoint_create: the adjoint runs FP32 populations");
+    if (p->quirks & (LBMX_QUIRK_REST_LAG | LBMX_QUIRK_IBM_2X2 | LBMX_QUIRK_IBM_CLAMP))
+        return afail(nullptr, LBMX_ERR_UNSUPPORTED,
+                     "lbmx_adjoint_create: quirks other than MRT_FORCE / ZOUHE_LEFT are not differentiated");
+    if (checkpoint_every < 1)
+        return afail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_create: checkpoint_every < 1");
+    if (cudaSetDevice(p->device) != cudaSuccess)
+        return afail(nullptr, LBMX_ERR_CUDA, "lbmx_adjoint_create: cannot select device %d", p->device);
+    lbmx_adjoint* a = new lbmx_adjoint();
+    a->p = *p;
+    a->n = (long long)p->nx * p->ny;
+    a->every = checkpoint_every;
+    a->blocks = grid_of(a->n);
+    memset(&a->args, 0, sizeof(a->args));
+    a->args.g = AdjGeom{p->nx, p->ny, p->periodic_x ? 1 : 0, p->periodic_y ? 1 : 0, a->n};
+    a->args.quirks = p->quirks;
+    a->args.omega = p->omega;
+    for (int k = 0; k < 9; k++) a->args.S[k] = p->S[k];
+    a->args.fx = p->body_fx;
+    a->args.fy = p->body_fy;
+    a->args.wall_ux = p->wall_ux;
+    a->args.wall_uy = p->wall_uy;
+    tie_omega(a);
+    std::vector<uint8_t> fl((size_t)a->n, 0);
+    if (flags && cudaMemcpy(fl.data(), flags, fl.size(), cudaMemcpyDefault) != cudaSuccess) {
+        delete a;
+        return afail(nullptr, LBMX_ERR_CUDA, "lbmx_adjoint_create: cannot read the flags");
+    }
+    if (check_flags(a, fl) != LBMX_OK) {
+        afail(nullptr, LBMX_ERR_UNSUPPORTED, "%s", a->err);
+        delete a;
+        return LBMX_ERR_UNSUPPORTED;
+    }
+    auto bail = [&](const char* what) {
+        afail(nullptr, LBMX_ERR_OUT_OF_MEMORY, "lbmx_adjoint_create: %s", what);
+        lbmx_adjoint_destroy(a);
+        return LBMX_ERR_OUT_OF_MEMORY;
+    };
+    const size_t state = (size_t)9 * a->n * sizeof(float);
+    if (cudaMalloc((void**)&a->flags, (size_t)a->n) != cudaSuccess ||
+        cudaMalloc((void**)&a->pc0, state) != cudaSuccess || cudaMalloc((void**)&a->ping[0], state) != cudaSuccess ||
+        cudaMalloc((void**)&a->ping[1], state) != cudaSuccess ||
+        cudaMalloc((void**)&a->jnode, (size_t)a->n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void**)&a->part, (size_t)a->blocks * 3 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void**)&a->avg_part, (size_t)a->blocks * 3 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void**)&a->red, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void**)&a->rho_out, (size_t)a->n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void**)&a->u_out, (size_t)2 * a->n * sizeof(float)) != cudaSuccess)
+        return bail("cudaMalloc failed");
+    if (p->stream) {
+        a->stream = (cudaStream_t)p->stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess) return bail("no stream");
+        a->own_stream = true;
+    }
+    cudaMemcpy(a->flags, fl.data(), fl.size(), cudaMemcpyHostToDevice);
+    a->args.flags = a->flags;
+    *out = a;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_set_state(lbmx_adjoint* a, const float* rho, const float* u) {
+    if (!a || !rho || !u) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_state: NULL argument");
+    cudaSetDevice(a->p.device);
+    float* tmp = nullptr;
+    ADJ_CUDA(a, cudaMalloc((void**)&tmp, (size_t)3 * a->n * sizeof(float)));
+    cudaMemcpyAsync(tmp, rho, (size_t)a->n * sizeof(float), cudaMemcpyDefault, a->stream);
+    cudaMemcpyAsync(tmp + a->n, u, (size_t)2 * a->n * sizeof(float), cudaMemcpyDefault, a->stream);
+    adj_init_kernel<<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(a->args.g, tmp, tmp + a->n, a->pc0);
+    const cudaError_t e = cudaStreamSynchronize(a->stream);
+    cudaFree(tmp);
+    ADJ_CUDA(a, e);
+    a->have_state = true;
+    a->have_forward = false;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_set_gamma(lbmx_adjoint* a, const float* gamma) {
+    if (!a) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_gamma: NULL handle");
+    cudaSetDevice(a->p.device);
+    if (!gamma) {
+        cudaFree(a->gamma);
+        a->gamma = nullptr;
+    } else {
+        if (!a->gamma) ADJ_CUDA(a, cudaMalloc((void**)&a->gamma, (size_t)a->n * sizeof(float)));
+        ADJ_CUDA(a, cudaMemcpyAsync(a->gamma, gamma, (size_t)a->n * sizeof(float), cudaMemcpyDefault, a->stream));
+        ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
+    }
+    a->args.gamma = a->gamma;
+    a->have_forward = false;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_set_scalars(lbmx_adjoint* a, float omega, float fx, float fy) {
+    if (!a) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_scalars: NULL handle");
+    for (int k = 0; k < 9; k++)
+        if ((a->args.omega_mask >> k) & 1u) a->args.S[k] = omega;
+    a->args.omega = omega;
+    a->args.fx = fx;
+    a->args.fy = fy;
+    a->have_forward = false;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_set_objective(lbmx_adjoint* a, const float* weights, int32_t first_step) {
+    if (!a || !weights) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_objective: NULL argument");
+    if (first_step < 1) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_objective: first_step < 1");
+    cudaSetDevice(a->p.device);
+    if (!a->weights) ADJ_CUDA(a, cudaMalloc((void**)&a->weights, (size_t)3 * a->n * sizeof(float)));
+    ADJ_CUDA(a, cudaMemcpyAsync(a->weights, weights, (size_t)3 * a->n * sizeof(float), cudaMemcpyDefault, a->stream));
+    ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
+    a->args.weights = a->weights;
+    a->first = first_step;
+    a->have_forward = false;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_forward(lbmx_adjoint* a, int32_t nsteps, double* objective) {
+    if (!a) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_forward: NULL handle");
+    if (!a->have_state) return afail(a, LBMX_ERR_NOT_INITIALIZED, "lbmx_adjoint_forward: call lbmx_adjoint_set_state first");
+    if (nsteps < 1) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_forward: nsteps < 1");
+    cudaSetDevice(a->p.device);
+    const size_t state = (size_t)9 * a->n;
+    const int ncheck = (nsteps + a->every - 1) / a->every;  // states at t = 0, every, 2 every, ...
+    if (ncheck > a->ncheck_cap) {
+        cudaFree(a->ckpt);
+        a->ckpt = nullptr;
+        ADJ_CUDA(a, cudaMalloc((void**)&a->ckpt, (size_t)ncheck * state * sizeof(float)));
+        a->ncheck_cap = ncheck;
+    }
+    if (nsteps + 1 > a->avg_cap) {
+        cudaFree(a->avg_hist);
+        a->avg_hist = nullptr;
+        ADJ_CUDA(a, cudaMalloc((void**)&a->avg_hist, (size_t)3 * (nsteps + 1) * sizeof(float)));
+        a->avg_cap = nsteps + 1;
+    }
+    ADJ_CUDA(a, cudaMemsetAsync(a->jnode, 0, (size_t)a->n * sizeof(double), a->stream));
+    ADJ_CUDA(a, cudaMemcpyAsync(a->ping[0], a->pc0, state * sizeof(float), cudaMemcpyDeviceToDevice, a->stream));
+    int cur = 0;
+    for (int t = 1; t <= nsteps; t++) {
+        if ((t - 1) % a->every == 0)
+            ADJ_CUDA(a, cudaMemcpyAsync(a->ckpt + (size_t)((t - 1) / a->every) * state, a->ping[cur],
+                                        state * sizeof(float), cudaMemcpyDeviceToDevice, a->stream));
+        lbmx_status st = forward_step(a, a->ping[cur], a->ping[cur ^ 1], t, t >= a->first, t == nsteps);
+        if (st != LBMX_OK) return st;
+        cur ^= 1;
+    }
+    adj_sum_kernel<<<1, kAdjBlock, 0, a->stream>>>(a->jnode, a->n, 1, a->red, 0);
+    ADJ_CUDA(a, cudaGetLastError());
+    double J = 0.0;
+    ADJ_CUDA(a, cudaMemcpyAsync(&J, a->red, sizeof(double), cudaMemcpyDeviceToHost, a->stream));
+    ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
+    if (objective) *objective = J;
+    a->T = nsteps;
+    a->have_forward = true;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_backward(lbmx_adjoint* a, float* grad_gamma, double* grad_scalars) {
+    if (!a) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_backward: NULL handle");
+    if (!a->have_forward)
+        return afail(a, LBMX_ERR_NOT_INITIALIZED, "lbmx_adjoint_backward: run lbmx_adjoint_forward with these inputs first");
+    cudaSetDevice(a->p.device);
+    const size_t state = (size_t)9 * a->n;
+    if (!a->seg) ADJ_CUDA(a, cudaMalloc((void**)&a->seg, (size_t)(a->every + 1) * state * sizeof(float)));
+    if (!a->lam[0]) {
+        ADJ_CUDA(a, cudaMalloc((void**)&a->lam[0], state * sizeof(float)));
+        ADJ_CUDA(a, cudaMalloc((void**)&a->lam[1], state * sizeof(float)));
+    }
+    if (!a->g_gamma) ADJ_CUDA(a, cudaMalloc((void**)&a->g_gamma, (size_t)a->n * sizeof(double)));
+    ADJ_CUDA(a, cudaMemsetAsync(a->g_gamma, 0, (size_t)a->n * sizeof(double), a->stream));
+    ADJ_CUDA(a, cudaMemsetAsync(a->part, 0, (size_t)a->blocks * 3 * sizeof(double), a->stream));
+    const bool opt = a->p.op == LBMX_CM_OPT;
+    const int T = a->T;
+    const int ncheck = (T + a->every - 1) / a->every;
+    int li = 0;
+    bool first_rev = true;
+    for (int c = ncheck - 1; c >= 0; c--) {
+        const int t0 = c * a->every, t1 = std::min(T, t0 + a->every);
+        // recompute the segment's states pc_t0 .. pc_t1
+        ADJ_CUDA(a, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)c * state, state * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, a->stream));
+        for (int t = t0 + 1; t <= t1; t++) {
+            const float* avg = opt ? a->avg_hist + (size_t)3 * t : nullptr;
+            const float* prev = a->seg + (size_t)(t - 1 - t0) * state;
+            float* next = a->seg + (size_t)(t - t0) * state;
+            ADJ_CUDA(a, op_dispatch(a->p.op, [&](auto opc) {
+                         adj_forward_kernel<decltype(opc)::value><<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(
+                             a->args, prev, next, avg, 0, nullptr, nullptr, nullptr);
+                         return cudaGetLastError();
+                     }));
+        }
+        for (int t = t1; t > t0; t--) {
+            const float* prev = a->seg + (size_t)(t - 1 - t0) * state;
+            const float* avg = opt ? a->avg_hist + (size_t)3 * t : nullptr;
+            const float* lam_next = first_rev ? nullptr : a->lam[li];
+            float* lam_out = a->lam[li ^ 1];
+            const int objective = t >= a->first ? 1 : 0;
+            ADJ_CUDA(a, op_dispatch(a->p.op, [&](auto opc) {
+                         adj_reverse_kernel<decltype(opc)::value><<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(
+                             a->args, prev, lam_next, lam_out, avg, objective, a->g_gamma, a->part, a->avg_part);
+                         return cudaGetLastError();
+                     }));
+            if (opt) {
+                adj_sum_kernel<<<1, kAdjBlock, 0, a->stream>>>(a->avg_part, a->blocks, 3, a->red + 4, 0);
+                ADJ_CUDA(a, cudaGetLastError());
+                adj_avg_back_kernel<<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(a->args, prev, a->red + 4, lam_out);
+                ADJ_CUDA(a, cudaGetLastError());
+            }
+            li ^= 1;
+            first_rev = false;
+        }
+    }
+    adj_sum_kernel<<<1, kAdjBlock, 0, a->stream>>>(a->part, a->blocks, 3, a->red, 0);
+    ADJ_CUDA(a, cudaGetLastError());
+    double g3[3];
+    ADJ_CUDA(a, cudaMemcpyAsync(g3, a->red, sizeof(g3), cudaMemcpyDeviceToHost, a->stream));
+    if (grad_gamma) {
+        float* tmp = a->lam[li ^ 1];  // free scratch
+        adj_to_float_kernel<<<grid_of(a->n), kAdjBlock, 0, a->stream>>>(a->g_gamma, tmp, a->n);
+        ADJ_CUDA(a, cudaGetLastError());
+        ADJ_CUDA(a, cudaMemcpyAsync(grad_gamma, tmp, (size_t)a->n * sizeof(float), cudaMemcpyDefault, a->stream));
+    }
+    ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
+    if (grad_scalars) {
+        grad_scalars[0] = g3[0];
+        grad_scalars[1] = g3[1];
+        grad_scalars[2] = g3[2];
+    }
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_moments(lbmx_adjoint* a, float* rho, float* u) {
+    if (!a) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_moments: NULL handle");
+    if (!a->have_forward) return afail(a, LBMX_ERR_NOT_INITIALIZED, "lbmx_adjoint_moments: no forward run");
+    cudaSetDevice(a->p.device);
+    if (rho) ADJ_CUDA(a, cudaMemcpyAsync(rho, a->rho_out, (size_t)a->n * sizeof(float), cudaMemcpyDefault, a->stream));
+    if (u) ADJ_CUDA(a, cudaMemcpyAsync(u, a->u_out, (size_t)2 * a->n * sizeof(float), cudaMemcpyDefault, a->stream));
+    ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
+    return LBMX_OK;
+}
+
+const char* lbmx_adjoint_last_error(lbmx_adjoint* a) { return a ? a->err : g_adj_err; }
+
+}  // extern "C"

@@ -83,6 +83,7 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.aux = h->aux;
     a.force = h->force;
     a.ibm_force = h->nm > 0 ? h->ibm_force : nullptr;
+    a.gamma = h->gamma;
     a.avg = h->avg;
     a.quirks = h->p.quirks;
     a.omega = h->p.omega;
@@ -93,7 +94,8 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.rho_out_bc = h->p.rho_out;
     a.body_fx = h->p.body_fx;
     a.body_fy = h->p.body_fy;
-    a.forced = (h->p.body_fx != 0.0f || h->p.body_fy != 0.0f || h->force != nullptr || h->nm > 0) ? 1 : 0;
+    a.forced = (h->p.body_fx != 0.0f || h->p.body_fy != 0.0f || h->force != nullptr || h->nm > 0 ||
+                h->gamma != nullptr) ? 1 : 0;
     a.special_units = h->special_units;
     a.nspecial = h->nspecial;
     a.special_chunks = h->special_chunks;
@@ -225,7 +227,7 @@ void lbmx_destroy(lbmx_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_ibm(h);
     cudaFree(h->f_alloc); cudaFree(h->flags); cudaFree(h->edge); cudaFree(h->aux);
-    cudaFree(h->force); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
+    cudaFree(h->force); cudaFree(h->gamma); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
     cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums);
     cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
     cudaFree(h->tile_counter); cudaFree(h->done_counter);
@@ -399,6 +401,27 @@ static lbmx_status upload_force(lbmx_handle* h, const float* force) {
         LBMX_CUDA(h, cudaMemcpy2DAsync(h->force + c * g.plane, g.pitch * sizeof(float), hf.data() + c * n,
                                        g.nx * sizeof(float), g.nx * sizeof(float), g.ny, cudaMemcpyHostToDevice,
                                        h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_set_brinkman(lbmx_handle* h, const float* gamma) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_brinkman: NULL handle");
+    cudaSetDevice(h->p.device);
+    const Geometry& g = h->g;
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (!gamma) {
+        cudaFree(h->gamma);
+        h->gamma = nullptr;
+        return LBMX_OK;
+    }
+    if (!h->gamma) {
+        cudaError_t e = cudaMalloc((void**)&h->gamma, (size_t)g.plane * sizeof(float));
+        if (e != cudaSuccess) return fail(h, LBMX_ERR_OUT_OF_MEMORY, "lbmx_set_brinkman: cudaMalloc failed");
+        LBMX_CUDA(h, cudaMemsetAsync(h->gamma, 0, (size_t)g.plane * sizeof(float), h->stream));
+    }
+    LBMX_CUDA(h, cudaMemcpy2DAsync(h->gamma, g.pitch * sizeof(float), gamma, g.nx * sizeof(float),
+                                   g.nx * sizeof(float), g.ny, cudaMemcpyDefault, h->stream));
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
     return LBMX_OK;
 }

@@ -415,18 +415,20 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
 // ---------------------------------------------------------------- collision
 // All operators take the post-stream (post-boundary) populations f, the
 // density, the force-corrected velocity and the force, and overwrite f with
-// the post-collision populations.  With OFS, f holds offsets f - w_q on entry
+// the post-collision populations.  The rates (omega, S) and the CM_OPT grid
+// averages have type P: float, or the adjoint's tangent type when gradients
+// with respect to them are wanted.  With OFS, f holds offsets f - w_q on entry
 // and on exit (rho is the full density): the weights' own moments are folded
 // into the equilibrium constants, so 16-bit storage needs no per-population
 // add on load or store.
 
 // BGK<2>::apply with Guo forcing -- BGK.cuh:15-39
-template <typename R, bool OFS = false>
-__device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R Fy, float omega, bool forced) {
+template <typename R, bool OFS = false, typename P = float>
+__device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R Fy, P omega, bool forced) {
     const R uu = fma(ux, ux, uy * uy);
     const R one = splat(1.0f, ux);
     const R base = fma(splat(-1.5f, ux), uu, one);
-    const float pref = 1.0f - 0.5f * omega;
+    const P pref = 1.0f - 0.5f * omega;
 #pragma unroll
     for (int q = 0; q < 9; q++) {
         const float cx = (float)CX(q), cy = (float)CY(q);
@@ -453,8 +455,8 @@ __device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R F
 // [rho, e, eps, jx, qx, jy, qy, pxx, pxy]; the equilibrium moments are
 // M f_eq of the second-order equilibrium in closed form; the back transform
 // uses M^-1 = M^T diag(1/|row|^2) (the rows are orthogonal).
-template <typename R, bool OFS = false>
-__device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R Fy, const float S[9],
+template <typename R, bool OFS = false, typename P = float>
+__device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R Fy, const P S[9],
                                             bool force_quirk, bool forced) {
     const R axis = (f[1] + f[2]) + (f[3] + f[4]);
     const R diag = (f[5] + f[6]) + (f[7] + f[8]);
@@ -529,8 +531,8 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
 // or the adapter rate `hor` for i > 5 (NoAdapter: use_hor = false), back
 // transform through raw moments (binomial shift) and the raw-moment basis
 // of D2Q9, the same linear map as the reference's closed-form T^-1(u).
-template <typename R, bool OFS = false>
-__device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy, const float S[9], R hor,
+template <typename R, bool OFS = false, typename P = float>
+__device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy, const P S[9], R hor,
                                            bool use_hor) {
     const R m10 = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const R m01 = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
@@ -605,10 +607,42 @@ __device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy
     f[8] = 0.25f * ((r12 + o22) - (r11 + r21));
 }
 
+// Initial populations f_eq(rho, u) (init_node, src/core/init/init.cuh:12-27):
+// second-order equilibrium, bracket in double as equilibrium.cu:13-38
+// evaluates it (cs^2 and cs^4 rounded to float first, as there); the
+// divisions become products with the reciprocals, computed once.
+__device__ __forceinline__ void init_equilibrium(float rho, float ux, float uy, float fe[9]) {
+    const float cs = 1.0f / sqrtf(3.0f);
+    const float cs2 = cs * cs, cs4 = cs2 * cs2;
+    const double inv_cs2 = 1.0 / (double)cs2, half_inv_cs4 = 0.5 / (double)cs4;
+    const float uu = ux * ux + uy * uy;
+    const double base = 1.0 - 0.5 * (double)uu * inv_cs2;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        const double cu = (double)((float)CX(q) * ux + (float)CY(q) * uy);
+        const double br = base + cu * cu * half_inv_cs4 + cu * inv_cs2;
+        fe[q] = (float)((double)(WQ(q) * rho) * br);
+    }
+}
+
+// Brinkman drag of a partially solid node (Guo & Zhao 2002, Darcy term):
+// F_B = -gamma rho u with u itself force-corrected, so
+// u = (j + F/2) / (rho (1 + gamma/2)) and the collision sees F + F_B.
+// gamma = 0 leaves u and F bit for bit unchanged.
+template <typename R>
+__device__ __forceinline__ void brinkman(R gm, R rho, R& ux, R& uy, R& Fx, R& Fy) {
+    const R sc = vdiv(splat(1.0f, rho), fma(splat(0.5f, rho), gm, splat(1.0f, rho)));
+    ux = ux * sc;
+    uy = uy * sc;
+    const R grho = gm * rho;
+    Fx = fma(-grho, ux, Fx);
+    Fy = fma(-grho, uy, Fy);
+}
+
 // OptimalAdapter::compute_higher_order_relaxation -- adapters.cuh:48-111
 // (Li et al. 2020 regression, theta* = (0.0003, -0.00775, 0.00016, 0.0087)).
-template <typename R>
-__device__ __forceinline__ R optimal_rate(R rho, R jmag, R pimag, const float* avg) {
+template <typename R, typename P = float>
+__device__ __forceinline__ R optimal_rate(R rho, R jmag, R pimag, const P* avg) {
     R ts = (0.0003f / avg[0]) * rho;
     ts = fma(splat(-0.00775f / avg[1], rho), jmag, ts);
     ts = fma(splat(0.00016f / avg[2], rho), pimag, ts);

@@ -22,6 +22,7 @@ struct lbmx_handle {
     float* aux = nullptr;          // [perimeter][9]
     float* force = nullptr;        // [2][plane] optional per-node body force
     float* ibm_force = nullptr;    // [2][plane]
+    float* gamma = nullptr;        // [plane] Brinkman solid fraction, null: none
     float* rho_out = nullptr;      // [plane]
     float* u_out = nullptr;        // [2][plane]
     float* staging = nullptr;      // dense [3][n] upload / readback staging

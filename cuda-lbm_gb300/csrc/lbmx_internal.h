@@ -34,6 +34,7 @@ struct StepArgs {
     const float* aux;        // [perimeter][9] neighbour data for ZG / pressure / corner
     const float* force;      // [2][plane] per-node body force or nullptr
     const float* ibm_force;  // [2][plane] IBM force (zero away from markers) or nullptr
+    const float* gamma;      // [plane] Brinkman solid fraction or nullptr
     const float* avg;        // CM_OPT grid averages {rho, |j|, |Pi|} (device)
     float* rho_out;          // [plane] moments written when non-null
     float* u_out;            // [2][plane]

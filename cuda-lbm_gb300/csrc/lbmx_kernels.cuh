@@ -129,8 +129,9 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, doubl
     node_force(a, off, &Fx, &Fy);
     // u = j/rho (macroscopics.cu:30-31), then u += F/(2 rho) (:106-107)
     const float inv = 1.0f / rho;
-    const float ux = jx * inv + 0.5f * Fx / rho;
-    const float uy = jy * inv + 0.5f * Fy / rho;
+    float ux = jx * inv + 0.5f * Fx / rho;
+    float uy = jy * inv + 0.5f * Fy / rho;
+    if (a.gamma) brinkman<float>(a.gamma[off], rho, ux, uy, Fx, Fy);
     float pimag = 0.f;
     if (OP == LBMX_CM_OPT || a.partials) {
         const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
@@ -306,8 +307,9 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         Fy.v = *reinterpret_cast<const float2*>(a.force + plane + off);
     }
     const V2 inv = vdiv(splat(1.0f, rho), rho);
-    const V2 ux = fma(0.5f * Fx, inv, jx * inv);
-    const V2 uy = fma(0.5f * Fy, inv, jy * inv);
+    V2 ux = fma(0.5f * Fx, inv, jx * inv);
+    V2 uy = fma(0.5f * Fy, inv, jy * inv);
+    if (a.gamma) brinkman<V2>(V2{*reinterpret_cast<const float2*>(a.gamma + off)}, rho, ux, uy, Fx, Fy);
     V2 pimag = splat(0.f, rho);
     if (OP == LBMX_CM_OPT || a.partials) {
         // offset form: sum c_x^2 w = sum c_y^2 w = 1/3
@@ -511,8 +513,9 @@ __global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a)
             float Fx, Fy;
             node_force(a, off, &Fx, &Fy);
             const float inv = 1.0f / rho;
-            const float ux = jx * inv + 0.5f * Fx / rho;
-            const float uy = jy * inv + 0.5f * Fy / rho;
+            float ux = jx * inv + 0.5f * Fx / rho;
+            float uy = jy * inv + 0.5f * Fy / rho;
+            if (a.gamma) brinkman<float>(a.gamma[off], rho, ux, uy, Fx, Fy);
             const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
             const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
             const float pxy = f[5] - f[6] + f[7] - f[8];
@@ -591,21 +594,8 @@ __global__ void init_kernel(const StepArgs a, const float* rho_in, const float* 
     const long long dn = (long long)y * a.g.nx + x;
     const long long off = (long long)y * a.g.pitch + x;
     const float rho = rho_in[dn], ux = u_in[dn], uy = u_in[n + dn];
-    // second-order equilibrium, bracket in double as equilibrium.cu:13-38
-    // evaluates it (cs^2 and cs^4 rounded to float first, as there); the
-    // divisions become products with the reciprocals, computed once
-    const float cs = 1.0f / sqrtf(3.0f);
-    const float cs2 = cs * cs, cs4 = cs2 * cs2;
-    const double inv_cs2 = 1.0 / (double)cs2, half_inv_cs4 = 0.5 / (double)cs4;
-    const float uu = ux * ux + uy * uy;
-    const double base = 1.0 - 0.5 * (double)uu * inv_cs2;
     float fe[9];
-#pragma unroll
-    for (int q = 0; q < 9; q++) {
-        const double cu = (double)((float)CX(q) * ux + (float)CY(q) * uy);
-        const double br = base + cu * cu * half_inv_cs4 + cu * inv_cs2;
-        fe[q] = (float)((double)(WQ(q) * rho) * br);
-    }
+    init_equilibrium(rho, ux, uy, fe);
     T* F = static_cast<T*>(a.f);
 #pragma unroll
     for (int q = 0; q < 9; q++) Store<T>::st(F + OPP(q) * a.g.plane + off, fe[q], WQ(q));

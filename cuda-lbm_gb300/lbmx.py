@@ -30,12 +30,15 @@ STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INV
           5: "NOT_INITIALIZED", 6: "UNSUPPORTED", 7: "NONFINITE", 8: "TOO_LARGE"}
 
 EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
-            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
+            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
             "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc", "lbmx_checkpoint_save",
             "lbmx_checkpoint_load", "lbmx_write_vti", "lbmx_batch_create", "lbmx_batch_destroy",
             "lbmx_batch_set_config", "lbmx_batch_get_config", "lbmx_batch_autotune", "lbmx_batch_step",
-            "lbmx_batch_synchronize", "lbmx_batch_last_error"]
+            "lbmx_batch_synchronize", "lbmx_batch_last_error", "lbmx_adjoint_create", "lbmx_adjoint_destroy",
+            "lbmx_adjoint_set_state", "lbmx_adjoint_set_gamma", "lbmx_adjoint_set_scalars",
+            "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward", "lbmx_adjoint_moments",
+            "lbmx_adjoint_last_error"]
 
 
 class Params(ctypes.Structure):
@@ -80,6 +83,8 @@ def load_library(path=LIB_PATH):
     lib.lbmx_set_flags.argtypes = [vp, vp]
     lib.lbmx_init_from_fields.argtypes = [vp, vp, vp, vp]
     lib.lbmx_set_force_field.argtypes = [vp, vp]
+    lib.lbmx_set_brinkman.argtypes = [vp, vp]
+    lib.lbmx_set_brinkman.restype = ctypes.c_int32
     lib.lbmx_step.argtypes = [vp, ctypes.c_int32]
     lib.lbmx_step_ex.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32]
     lib.lbmx_moments.argtypes = [vp, vp, vp, dp]
@@ -106,6 +111,21 @@ def load_library(path=LIB_PATH):
     lib.lbmx_batch_last_error.argtypes = [vp]
     for name in ("lbmx_batch_create", "lbmx_batch_set_config", "lbmx_batch_get_config", "lbmx_batch_autotune",
                  "lbmx_batch_step", "lbmx_batch_synchronize"):
+        getattr(lib, name).restype = ctypes.c_int32
+    lib.lbmx_adjoint_create.argtypes = [P(Params), vp, ctypes.c_int32, P(vp)]
+    lib.lbmx_adjoint_destroy.argtypes = [vp]
+    lib.lbmx_adjoint_set_state.argtypes = [vp, vp, vp]
+    lib.lbmx_adjoint_set_gamma.argtypes = [vp, vp]
+    lib.lbmx_adjoint_set_scalars.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+    lib.lbmx_adjoint_set_objective.argtypes = [vp, vp, ctypes.c_int32]
+    lib.lbmx_adjoint_forward.argtypes = [vp, ctypes.c_int32, dp]
+    lib.lbmx_adjoint_backward.argtypes = [vp, vp, dp]
+    lib.lbmx_adjoint_moments.argtypes = [vp, vp, vp]
+    lib.lbmx_adjoint_last_error.restype = ctypes.c_char_p
+    lib.lbmx_adjoint_last_error.argtypes = [vp]
+    for name in ("lbmx_adjoint_create", "lbmx_adjoint_set_state", "lbmx_adjoint_set_gamma", "lbmx_adjoint_set_scalars",
+                 "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward",
+                 "lbmx_adjoint_moments"):
         getattr(lib, name).restype = ctypes.c_int32
     lib.lbmx_moment_sums_noalloc.restype = ctypes.c_int32
     lib.lbmx_moment_sums_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
@@ -190,6 +210,10 @@ class Lattice:
         pu, k2 = _ptr(u, np.float32)
         pf, k3 = _ptr(force, np.float32)
         self._check(self.lib.lbmx_init_from_fields(self.h, pr, pu, pf))
+
+    def set_brinkman(self, gamma):
+        pg, k = _ptr(gamma, np.float32)
+        self._check(self.lib.lbmx_set_brinkman(self.h, pg))
 
     def set_force_field(self, force):
         pf, k = _ptr(force, np.float32)
@@ -295,3 +319,82 @@ class Batch:
 
     def synchronize(self):
         self._check(self.lib.lbmx_batch_synchronize(self.b))
+
+
+class Adjoint:
+    """Discrete adjoint of the step (lbmx_adjoint_*): J over steps >= first of
+    w_rho rho + w_x rho u_x + w_y rho u_y, and its gradient with respect to
+    the Brinkman field gamma, omega and the body force."""
+
+    def __init__(self, nx, ny, op=BGK, omega=1.0, S=None, periodic=(False, False), flags=None, checkpoint_every=1,
+                 quirks=0, wall_u=(0.0, 0.0), body_force=(0.0, 0.0), device=0, stream=None):
+        self.lib = lib()
+        p = Params()
+        self.lib.lbmx_params_default(ctypes.byref(p))
+        p.nx, p.ny = nx, ny
+        p.periodic_x, p.periodic_y = int(bool(periodic[0])), int(bool(periodic[1]))
+        p.op, p.quirks, p.device, p.omega = op, quirks, device, omega
+        S = [omega] * 9 if S is None else S
+        for i in range(9):
+            p.S[i] = S[i]
+        p.wall_ux, p.wall_uy = wall_u
+        p.body_fx, p.body_fy = body_force
+        p.stream = stream
+        fl = np.zeros((ny, nx), np.uint8) if flags is None else np.ascontiguousarray(flags, np.uint8)
+        a = ctypes.c_void_p()
+        rc = self.lib.lbmx_adjoint_create(ctypes.byref(p), fl.ctypes.data, int(checkpoint_every), ctypes.byref(a))
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_adjoint_last_error(None).decode())
+        self.a = a
+        self.nx, self.ny, self.n = nx, ny, nx * ny
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_adjoint_last_error(self.a).decode())
+
+    def close(self):
+        if getattr(self, "a", None):
+            self.lib.lbmx_adjoint_destroy(self.a)
+            self.a = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, rho, u):
+        pr, k1 = _ptr(rho, np.float32)
+        pu, k2 = _ptr(u, np.float32)
+        self._check(self.lib.lbmx_adjoint_set_state(self.a, pr, pu))
+
+    def set_gamma(self, gamma):
+        pg, k = _ptr(gamma, np.float32)
+        self._check(self.lib.lbmx_adjoint_set_gamma(self.a, pg))
+
+    def set_scalars(self, omega, fx, fy):
+        self._check(self.lib.lbmx_adjoint_set_scalars(self.a, float(omega), float(fx), float(fy)))
+
+    def set_objective(self, weights, first_step):
+        pw, k = _ptr(weights, np.float32)
+        self._check(self.lib.lbmx_adjoint_set_objective(self.a, pw, int(first_step)))
+
+    def forward(self, nsteps):
+        J = ctypes.c_double()
+        self._check(self.lib.lbmx_adjoint_forward(self.a, int(nsteps), ctypes.byref(J)))
+        return J.value
+
+    def backward(self, grad_gamma=None):
+        """(dJ/dgamma [ny, nx], (dJ/domega, dJ/dFx, dJ/dFy)); grad_gamma may be a
+        float32 CUDA tensor to receive dJ/dgamma in place."""
+        g3 = (ctypes.c_double * 3)()
+        if grad_gamma is None:
+            out = np.empty((self.ny, self.nx), np.float32)
+            self._check(self.lib.lbmx_adjoint_backward(self.a, out.ctypes.data, g3))
+        else:
+            out = grad_gamma
+            self._check(self.lib.lbmx_adjoint_backward(self.a, out.data_ptr(), g3))
+        return out, tuple(g3)
+
+    def moments(self):
+        rho = np.empty((self.ny, self.nx), np.float32)
+        u = np.empty((2, self.ny, self.nx), np.float32)
+        self._check(self.lib.lbmx_adjoint_moments(self.a, rho.ctypes.data, u.ctypes.data))
+        return rho, u

@@ -150,6 +150,12 @@ lbmx_status lbmx_set_force_field(lbmx_handle* h, const float* force);
 lbmx_status lbmx_step(lbmx_handle* h, int32_t nsteps);
 lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags);
 
+/* No counterpart in the reference.  Per-node Brinkman solid fraction
+ * gamma[n] (NULL: none): a Darcy drag F_B = -gamma rho u acts with the body
+ * force (Guo & Zhao 2002), u = (j + F/2) / (rho (1 + gamma/2)); gamma = 0 is
+ * open fluid, gamma = 1 damps the velocity by a third each step. */
+lbmx_status lbmx_set_brinkman(lbmx_handle* h, const float* gamma);
+
 /* Replaces LBM::update_macroscopics (src/core/lbm.cuh:148-154): the last
  * stored step's density rho[n] and force-corrected velocity u[2n] (the
  * reference's d_rho / d_u), and FP64 sums {rho, rho*ux, rho*uy}.  Any output
@@ -220,6 +226,38 @@ const char* lbmx_last_error(lbmx_handle* h);
  * streams with no ordering between them) race and must not be made. */
 #define LBMX_NOALLOC_MAX_NODES 2147483647LL
 lbmx_status lbmx_moment_sums_noalloc(const float* rho, const float* u, int64_t n, double* sums3, void* stream);
+
+/* ------------------------------------------------------------------ adjoint
+ * No counterpart in the reference.  Gradients of an objective of the step's
+ * moments,
+ *     J = sum over steps t >= first_step and nodes x of
+ *         w_rho(x) rho_t(x) + w_x(x) rho_t u_x,t(x) + w_y(x) rho_t u_y,t(x),
+ * with respect to the per-node Brinkman field gamma, the relaxation rate
+ * omega (with every S entry equal to omega at creation) and the uniform body
+ * force, by a discrete adjoint of the step: forward-mode tangents through the
+ * per-node boundary / Brinkman / collision code give each node's Jacobian
+ * exactly, and the populations are recomputed from checkpoints taken every
+ * `checkpoint_every` steps, so memory is (steps / every + every) states.
+ * FP32 populations; any operator; fluid, bounce-back (where it reads no
+ * population from outside the domain) and half-way / moving walls; no IBM. */
+typedef struct lbmx_adjoint lbmx_adjoint;
+
+lbmx_status lbmx_adjoint_create(const lbmx_params* p, const uint8_t* flags, int32_t checkpoint_every,
+                                lbmx_adjoint** out);
+void lbmx_adjoint_destroy(lbmx_adjoint* a);
+/* initial rho[n], u[2n] (populations start at equilibrium, as lbmx_init_from_fields) */
+lbmx_status lbmx_adjoint_set_state(lbmx_adjoint* a, const float* rho, const float* u);
+lbmx_status lbmx_adjoint_set_gamma(lbmx_adjoint* a, const float* gamma);
+lbmx_status lbmx_adjoint_set_scalars(lbmx_adjoint* a, float omega, float body_fx, float body_fy);
+/* weights[3n]: w_rho, w_x, w_y planes */
+lbmx_status lbmx_adjoint_set_objective(lbmx_adjoint* a, const float* weights, int32_t first_step);
+/* nsteps steps from the initial state; J into *objective */
+lbmx_status lbmx_adjoint_forward(lbmx_adjoint* a, int32_t nsteps, double* objective);
+/* dJ/dgamma[n] (may be NULL) and {dJ/domega, dJ/dFx, dJ/dFy} of the last forward run */
+lbmx_status lbmx_adjoint_backward(lbmx_adjoint* a, float* grad_gamma, double* grad_scalars);
+/* rho[n], u[2n] of the last forward step */
+lbmx_status lbmx_adjoint_moments(lbmx_adjoint* a, float* rho, float* u);
+const char* lbmx_adjoint_last_error(lbmx_adjoint* a);
 
 /* ------------------------------------------------------------------ batches
  * No counterpart in the reference, which runs one lattice per process

@@ -68,6 +68,7 @@ struct lbo {
     real *rho, *ux, *uy, *pimag;
     real *fx, *fy;       /* LBM force */
     real *bfx, *bfy;     /* body force from Init::apply_forces */
+    real *gamma;         /* Brinkman solid fraction, NULL: none (no reference counterpart) */
     real *aux;           /* [9][n] neighbour data for ZG / pressure / corner boundaries */
     uint8_t *flags;
     int has_aux_bc;
@@ -120,7 +121,7 @@ void lbo_destroy(lbo* o) {
     if (!o) return;
     free(o->f); free(o->fb); free(o->feq); free(o->aux);
     free(o->rho); free(o->ux); free(o->uy); free(o->pimag);
-    free(o->fx); free(o->fy); free(o->bfx); free(o->bfy); free(o->flags);
+    free(o->fx); free(o->fy); free(o->bfx); free(o->bfy); free(o->flags); free(o->gamma);
     free_markers(o);
     free(o);
 }
@@ -600,6 +601,20 @@ static void collide_cm(const lbo* o, long nd) {
 
 /* ---------------------------------------------------------------- driver */
 
+/* Brinkman drag F_B = -gamma rho u of a partially solid node (Guo & Zhao
+ * 2002), no reference counterpart: u = (j + F/2) / (rho (1 + gamma/2)) and
+ * the collision sees F + F_B.  NULL removes the field. */
+int lbo_set_gamma(lbo* o, const double* gamma) {
+    if (!gamma) {
+        free(o->gamma);
+        o->gamma = NULL;
+        return 0;
+    }
+    if (!o->gamma) o->gamma = (real*)xcalloc(o->n, sizeof(real));
+    for (long i = 0; i < o->n; i++) o->gamma[i] = (real)gamma[i];
+    return 0;
+}
+
 int lbo_init(lbo* o, const double* rho, const double* u, const double* force) {
     const long n = o->n;
     for (long i = 0; i < n; i++) {
@@ -703,6 +718,14 @@ static void one_step(lbo* o) {
         real r = o->rho[nd];
         o->ux[nd] += (real)0.5 * o->fx[nd] / r;
         o->uy[nd] += (real)0.5 * o->fy[nd] / r;
+        if (o->gamma) {
+            const real g = o->gamma[nd];
+            const real sc = (real)1 / ((real)0.5 * g + (real)1);
+            o->ux[nd] *= sc;
+            o->uy[nd] *= sc;
+            o->fx[nd] -= g * r * o->ux[nd];
+            o->fy[nd] -= g * r * o->uy[nd];
+        }
         s0 += (double)r;
         s1 += (double)r * (double)o->ux[nd];
         s2 += (double)r * (double)o->uy[nd];

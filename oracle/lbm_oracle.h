@@ -86,6 +86,8 @@ int   lbo_set_flags(lbo* o, const uint8_t* flags);
 /* rho[n], u[2n], force[2n] (force = Init::apply_forces result, re-applied each step) */
 int   lbo_init(lbo* o, const double* rho, const double* u, const double* force);
 int   lbo_set_markers(lbo* o, const double* xy, int n);   /* xy AoS [2n] */
+/* per-node Brinkman solid fraction gamma[n] (NULL: none); no reference counterpart */
+int   lbo_set_gamma(lbo* o, const double* gamma);
 int   lbo_step(lbo* o, int nsteps);
 long  lbo_time(const lbo* o);
 /* post-collision populations of the last step, [9][n] */

@@ -52,6 +52,7 @@ def _lib(precision):
         lib.lbo_set_flags.argtypes = [ctypes.c_void_p, P(ctypes.c_uint8)]
         lib.lbo_init.argtypes = [ctypes.c_void_p, dp, dp, dp]
         lib.lbo_set_markers.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
+        lib.lbo_set_gamma.argtypes = [ctypes.c_void_p, dp]
         lib.lbo_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.lbo_time.restype = ctypes.c_long
         lib.lbo_time.argtypes = [ctypes.c_void_p]
@@ -110,6 +111,14 @@ class Oracle:
         xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
         self.nm = xy.size // 2
         self.lib.lbo_set_markers(self.h, _dp(xy), self.nm)
+
+    def set_gamma(self, gamma):
+        if gamma is None:
+            self.lib.lbo_set_gamma(self.h, None)
+            return
+        g = np.ascontiguousarray(gamma, dtype=np.float64).reshape(-1)
+        assert g.size == self.n
+        self.lib.lbo_set_gamma(self.h, _dp(g))
 
     def step(self, n=1):
         self.lib.lbo_step(self.h, int(n))

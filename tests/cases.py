@@ -161,3 +161,42 @@ def ensemble(count=512, seed=0, sides=tuple(range(64, 769, 32)), re_range=(100.0
 def ensemble_cavity(side, nu, op=MRT, u_lid=0.1):
     """One cavity of the ensemble: rho = 1, u = 0, half-way walls, moving lid."""
     return cavity_moving_wall(side, side, op=op, nu=nu, u_lid=u_lid)
+
+
+def splitmix64(z):
+    """splitmix64 finaliser on a uint64 array (counter-based normal noise)."""
+    z = np.asarray(z, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def brinkman_field(nx, ny, sigma=16.0, seed=0):
+    """Per-node solid fraction in [0, 1]: i.i.d. N(0, 1) per node from a
+    splitmix64 counter hash (Box-Muller), Gaussian-blurred with sigma nodes
+    (periodic in x, reflected in y), min-max scaled."""
+    from scipy.ndimage import gaussian_filter
+    i = np.arange(nx * ny, dtype=np.uint64) + np.uint64(seed) * np.uint64(2 * nx * ny)
+    a = splitmix64(np.uint64(2) * i)
+    b = splitmix64(np.uint64(2) * i + np.uint64(1))
+    u1 = ((a >> np.uint64(11)).astype(np.float64) + 0.5) * 2.0 ** -53
+    u2 = (b >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    z = (np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)).reshape(ny, nx)
+    s = gaussian_filter(z, sigma, mode=("reflect", "wrap"))
+    return ((s - s.min()) / (s.max() - s.min())).astype(np.float32)
+
+
+def channel_brinkman(nx=64, ny=32, op=CM_OPT, nu=0.02, u_max=0.05, sigma=16.0, gamma_scale=1.0, seed=0, **kw):
+    """Body-force Poiseuille channel with a Brinkman field: periodic x,
+    half-way bounce-back walls at y = 0 and y = ny - 1 (the walls half a link
+    outside), F_x = 8 nu u_max / ny^2 (poiseuilleFunctors.cuh:37)."""
+    fl = np.zeros((ny, nx), np.uint8)
+    fl[0, :] = HALFWAY_BB
+    fl[-1, :] = HALFWAY_BB
+    F = np.zeros((2, ny, nx))
+    F[0] = 8.0 * nu * u_max / (ny * ny)
+    c = base(nx, ny, op, nu, periodic=(True, False), flags=fl, force=F, **kw)
+    c["gamma"] = gamma_scale * brinkman_field(nx, ny, sigma=sigma, seed=seed)
+    return c

@@ -105,3 +105,22 @@ def test_ibm_force_opposes_flow():
     o.step(200)
     _, _, F = o.markers()
     assert F[0].sum() < 0  # drag on the fluid points upstream
+
+
+def test_oracle_brinkman_term():
+    # gamma = 0 is the plain step bit for bit; a solid fraction slows the channel
+    c = C.channel_brinkman(32, 16, op=C.BGK, sigma=2.0, gamma_scale=0.5)
+    assert 0.0 <= c["gamma"].min() and c["gamma"].max() <= 0.5 + 1e-7
+    o1 = C.make_oracle(c)
+    o1.step(40)
+    _, u1, _ = o1.moments()
+    o0 = C.make_oracle(c)
+    o0.set_gamma(np.zeros_like(c["gamma"]))
+    o0.step(40)
+    _, u0, _ = o0.moments()
+    np.testing.assert_array_equal(u0, u1)
+    o2 = C.make_oracle(c)
+    o2.set_gamma(c["gamma"])
+    o2.step(40)
+    _, u2, _ = o2.moments()
+    assert u2[0].mean() < 0.9 * u1[0].mean()
