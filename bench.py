@@ -24,6 +24,10 @@ half-way moving wall, half-way bounce-back on the other walls, Re = 1000
             step (CUDA graphs, autotuned tile shape), aggregate MLUPS for
             FP16-offset and FP32 storage and the per-instance L2 velocity
             error of the smallest instances against the FP64 oracle.
+  adjoint   the discrete adjoint on the Brinkman channel (4096 x 1024,
+            5000 steps, checkpoint every 250): forward and backward times,
+            the gradients of the outlet mass flux, and a bounded check
+            against FP64 central differences of the oracle.
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on the same
             workload, 200 steps.
 
@@ -257,6 +261,99 @@ def bench_ensemble(args, torch, stream, device, hbm):
     return out
 
 
+def bench_adjoint(args, torch, stream, device):
+    """Adjoint of the outlet mass flux (time average over the run) of the
+    body-force Brinkman channel: 4096 x 1024, periodic x, half-way bounce-back
+    walls, nu 0.02, F_x = 8 nu u_max / ny^2 for u_max 0.05, per-node solid
+    fraction gamma in [0, 1] (splitmix64 normal noise, Gaussian blur sigma 16,
+    min-max), 5000 steps with a checkpoint every 250, FP32.  CM<NoAdapter>:
+    CM<OptimalAdapter> diverges on this flow (the adapter's rate runs away
+    once the drag has damped |u| to ~1e-5; the FP64 oracle's run goes
+    non-finite near step 110), which the line records.  A bounded check runs
+    the same flow at 256 x 64 for 400 steps against FP64 central differences
+    of the oracle."""
+    import cases as C
+    import lbmx
+    nx, ny, T, K = args.adj_nx, args.adj_ny, args.adj_steps, args.adj_every
+
+    def build(op, nx_, ny_, every, sigma):
+        c = C.channel_brinkman(nx_, ny_, op=op, nu=0.02, u_max=0.05, sigma=sigma, gamma_scale=1.0, seed=0)
+        fx = float(c["force"][0].flat[0])
+        a = lbmx.Adjoint(nx_, ny_, op=op, omega=c["omega"], S=c["S"], periodic=c["periodic"], flags=c["flags"],
+                         checkpoint_every=every, body_force=(fx, 0.0), device=device, stream=stream.cuda_stream)
+        a.set_state(np.ones((ny_, nx_), np.float32), np.zeros((2, ny_, nx_), np.float32))
+        a.set_gamma(c["gamma"])
+        return c, a
+
+    def flux_weights(nx_, ny_, steps):
+        w = np.zeros((3, ny_, nx_), np.float32)
+        w[1, :, nx_ - 1] = 1.0 / steps
+        return w
+
+    c, a = build(C.CM, nx, ny, K, 16.0)
+    a.set_objective(flux_weights(nx, ny, T), 1)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record(stream)
+    J = a.forward(T)
+    e[1].record(stream)
+    g_gamma, (g_om, g_fx, g_fy) = a.backward()
+    e[2].record(stream)
+    stream.synchronize()
+    fwd_ms, bwd_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    out = {"workload": "Brinkman channel %dx%d, D2Q9 CM, periodic x, half-way walls, nu 0.02, u_max 0.05, "
+                       "gamma in [0,1] (sigma 16), outlet mass flux averaged over %d steps" % (nx, ny, T),
+           "steps": T, "checkpoint_every": K, "J": J, "forward_s": round(fwd_ms / 1e3, 3),
+           "backward_s": round(bwd_ms / 1e3, 3),
+           "backward_MLUPS": round(nx * ny * T / (bwd_ms * 1e-3) / 1e6, 1),
+           "dJ_domega": g_om, "dJ_dFx": g_fx, "dJ_dFy": g_fy,
+           "dJ_dgamma": {"l2": float(np.sqrt((g_gamma.astype(np.float64) ** 2).sum())),
+                         "min": float(g_gamma.min()), "max": float(g_gamma.max()),
+                         "finite": bool(np.isfinite(g_gamma).all())},
+           "device_memory_GB": round((9 * nx * ny * 4 * ((T + K - 1) // K + K + 1 + 5)) / 1e9, 2)}
+    del a
+    c_opt, a_opt = build(C.CM_OPT, nx, ny, K, 16.0)
+    a_opt.set_objective(flux_weights(nx, ny, T), 1)
+    J_opt = a_opt.forward(T)
+    out["cm_opt"] = {"J": J_opt if np.isfinite(J_opt) else None, "finite": bool(np.isfinite(J_opt))}
+    del a_opt
+    # bounded FP64 central-difference check
+    import oracle as O
+    snx, sny, sT = 256, 64, 400
+    cs, a = build(C.CM, snx, sny, 50, 4.0)
+    w = flux_weights(snx, sny, sT)
+    a.set_objective(w, 1)
+    a.forward(sT)
+    gg, (gw, gfx, _) = a.backward()
+    om, fx = cs["omega"], float(cs["force"][0].flat[0])
+    gam = cs["gamma"].astype(np.float64)
+
+    def J64(gamma, omega, force_x):
+        o = O.Oracle(snx, sny, op=C.CM, omega=omega, S=C.S_for(C.CM, omega), periodic=(True, False),
+                     precision="f64", threads=os.cpu_count() or 1)
+        o.set_flags(cs["flags"])
+        o.set_gamma(gamma)
+        F = np.zeros((2, sny, snx))
+        F[0] = force_x
+        o.init(np.ones((sny, snx)), np.zeros((2, sny, snx)), F)
+        acc = 0.0
+        for _ in range(sT):
+            o.step(1)
+            r, u, _ = o.moments()
+            acc += float((w[1] * r * u[0]).sum())
+        return acc
+
+    d = C.brinkman_field(snx, sny, sigma=3.0, seed=7).astype(np.float64) - 0.5
+    fd_om = (J64(gam, om + 1e-4, fx) - J64(gam, om - 1e-4, fx)) / 2e-4
+    fd_fx = (J64(gam, om, fx * (1 + 1e-3)) - J64(gam, om, fx * (1 - 1e-3))) / (2e-3 * fx)
+    fd_g = (J64(gam + 1e-6 * d, om, fx) - J64(gam - 1e-6 * d, om, fx)) / 2e-6
+    ad_g = float((gg.astype(np.float64) * d).sum())
+    rel = lambda x, y: abs(x - y) / max(abs(y), 1e-300)
+    out["fd_check"] = {"workload": "same flow, %dx%d, %d steps" % (snx, sny, sT), "reference": "FP64 oracle",
+                       "rel_err_omega": rel(gw, fd_om), "rel_err_Fx": rel(gfx, fd_fx),
+                       "rel_err_gamma_direction": rel(ad_g, fd_g)}
+    return out
+
+
 def bench_reference(args, rank, world):
     """CPU implementation of the reference step (the oracle port), all host threads."""
     if rank != 0:
@@ -303,6 +400,10 @@ def main():
     ap.add_argument("--ens-steps", type=int, default=64)
     ap.add_argument("--ens-err-count", type=int, default=6)
     ap.add_argument("--ens-err-steps", type=int, default=1000)
+    ap.add_argument("--adj-nx", type=int, default=4096)
+    ap.add_argument("--adj-ny", type=int, default=1024)
+    ap.add_argument("--adj-steps", type=int, default=5000)
+    ap.add_argument("--adj-every", type=int, default=250)
     ap.add_argument("--quick", action="store_true", help="main number only (profiling runs)")
     ap.add_argument("--storage", default="f32", choices=["f32", "f16_offset", "bf16_offset"],
                     help="storage of the main lattice with --quick (profiling runs)")
@@ -448,6 +549,8 @@ def main():
         }
         # ---- batched ensemble (many lattices, one persistent launch per step)
         line["ensemble"] = bench_ensemble(args, torch, stream, local, hbm)
+        # ---- adjoint of the Brinkman channel
+        line["adjoint"] = bench_adjoint(args, torch, stream, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -3,7 +3,8 @@
 // respect to the per-node Brinkman field gamma, the relaxation rate omega and
 // the body force, by checkpointed recomputation.
 //
-// Forward model (the engine's step, written densely with ping-pong buffers):
+// Forward model (the engine's step, written densely with ping-pong buffers,
+// populations held as offsets f - w_q in FP32):
 //   ps_t[x][q] = pc_{t-1}[x - c_q][q]          streaming (periodic wrap);
 //                pc_{t-1}[x][OPP q] - W(OPP q)  half-way wall node, link out
 //   fb_t = B(ps_t)                             on-node bounce-back (flag 1)
@@ -102,9 +103,15 @@ __device__ __forceinline__ void adj_bc(const AdjGeom& g, R f[9], int x, int y, u
     }
 }
 
+// The adjoint carries populations as offsets f - w_q (the engine's 16-bit
+// form, here in FP32): at the low Mach numbers of a drag-damped flow, FP32
+// then resolves the deviation from rest instead of the weights.  Half-way
+// reflection and on-node bounce-back copy between opposite directions, whose
+// weights are equal, so they act on offsets unchanged.
+
 // density and force-corrected, Brinkman-corrected velocity, as general_node
 template <typename R>
-__device__ __forceinline__ void adj_macro(const R f[9], R gm, R& Fx, R& Fy, R& rho, R& ux, R& uy) {
+__device__ __forceinline__ void adj_macro(const R f[9], R gm, R& Fx, R& Fy, R& rho, R& drho, R& ux, R& uy) {
     rho = f[0];
     R jx = splat(0.0f, f[0]), jy = splat(0.0f, f[0]);
 #pragma unroll
@@ -115,6 +122,8 @@ __device__ __forceinline__ void adj_macro(const R f[9], R gm, R& Fx, R& Fy, R& r
         if (CY(q) == 1) jy = jy + f[q];
         if (CY(q) == -1) jy = jy - f[q];
     }
+    drho = rho;                    // rho - 1, exactly
+    rho = rho + splat(1.0f, rho);  // the weights sum to 1
     const R inv = vdiv(splat(1.0f, rho), rho);
     ux = jx * inv + vdiv(0.5f * Fx, rho);
     uy = jy * inv + vdiv(0.5f * Fy, rho);
@@ -123,7 +132,8 @@ __device__ __forceinline__ void adj_macro(const R f[9], R gm, R& Fx, R& Fy, R& r
 
 template <typename R>
 __device__ __forceinline__ R adj_pimag(const R f[9]) {
-    const R d = ((f[5] + f[6]) + f[7]) + f[8];
+    // sum c_x^2 w = sum c_y^2 w = 1/3
+    const R d = (((f[5] + f[6]) + f[7]) + f[8]) + splat(1.0f / 3.0f, f[0]);
     const R pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
     const R pxy = ((f[5] - f[6]) + f[7]) - f[8];
     return vsqrt(fma(pxx, pxx, fma(2.0f * pxy, pxy, pyy * pyy)));
@@ -133,29 +143,29 @@ __device__ __forceinline__ R adj_pimag(const R f[9]) {
 template <typename R, int OP>
 __device__ __forceinline__ void adj_node(const AdjArgs& a, R f[9], R gm, R Fx, R Fy, R omega, const R S[9],
                                          const R avg[3], R mom[3]) {
-    R rho, ux, uy;
-    adj_macro<R>(f, gm, Fx, Fy, rho, ux, uy);
+    R rho, drho, ux, uy;
+    adj_macro<R>(f, gm, Fx, Fy, rho, drho, ux, uy);
     mom[0] = rho;
     mom[1] = ux;
     mom[2] = uy;
     if (OP == LBMX_BGK) {
-        collide_bgk<R, false, R>(f, rho, ux, uy, Fx, Fy, omega, true);
+        collide_bgk<R, true, R>(f, rho, drho, ux, uy, Fx, Fy, omega, true);
     } else if (OP == LBMX_MRT) {
-        collide_mrt<R, false, R>(f, rho, ux, uy, Fx, Fy, S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, true);
+        collide_mrt<R, true, R>(f, rho, drho, ux, uy, Fx, Fy, S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, true);
     } else if (OP == LBMX_CM) {
-        collide_cm<R, false, R>(f, rho, ux, uy, Fx, Fy, S, rho, false);
+        collide_cm<R, true, R>(f, rho, drho, ux, uy, Fx, Fy, S, rho, false);
     } else {
         const R pimag = adj_pimag<R>(f);
         const R jmag = vsqrt(fma(ux, ux, uy * uy)) * rho;
-        collide_cm<R, false, R>(f, rho, ux, uy, Fx, Fy, S, optimal_rate<R, R>(rho, jmag, pimag, avg), true);
+        collide_cm<R, true, R>(f, rho, drho, ux, uy, Fx, Fy, S, optimal_rate<R, R>(rho, jmag, pimag, avg), true);
     }
 }
 
 // the node's terms of the CM_OPT grid averages: rho, rho |u|, |Pi|
 template <typename R>
 __device__ __forceinline__ void adj_avg_terms(const R f[9], R gm, R Fx, R Fy, R out[3]) {
-    R rho, ux, uy;
-    adj_macro<R>(f, gm, Fx, Fy, rho, ux, uy);
+    R rho, drho, ux, uy;
+    adj_macro<R>(f, gm, Fx, Fy, rho, drho, ux, uy);
     out[0] = rho;
     out[1] = rho * vsqrt(fma(ux, ux, uy * uy));
     out[2] = adj_pimag<R>(f);
@@ -188,7 +198,7 @@ __global__ void adj_init_kernel(AdjGeom g, const float* rho, const float* u, flo
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
     float fe[9];
-    init_equilibrium(rho[i], u[i], u[g.n + i], fe);
+    init_equilibrium<true>(rho[i], u[i], u[g.n + i], fe);
 #pragma unroll
     for (int q = 0; q < 9; q++) pc[q * g.n + i] = fe[q];
 }
@@ -265,6 +275,18 @@ __global__ void __launch_bounds__(kAdjBlock) adj_reverse_kernel(const AdjArgs a,
             }
             mu[q] = m;
         }
+        // The collision conserves mass, so a column's tangents sum to an
+        // integer -- 0 for the parameters, 1 (or more where bounce-back copies
+        // a population) for a population -- while mu is nearly constant over
+        // q.  Dotting mu - mean(mu) and adding mean(mu) times that integer
+        // keeps FP32 from cancelling mean(mu) against the rounding of the
+        // tangents.
+        float c = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) c += mu[q];
+        c *= 1.0f / 9.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) mu[q] -= c;
         float ps[9];
         adj_gather(a, pc_prev, x, y, node, fl, ps);
         float w[3] = {0.0f, 0.0f, 0.0f};
@@ -301,8 +323,13 @@ __global__ void __launch_bounds__(kAdjBlock) adj_reverse_kernel(const AdjArgs a,
             for (int k = 0; k < kTan; k++) {
                 if (p0 + k >= D) break;
                 float t = w[0] * mom[0].d[k] + w[1] * jx.d[k] + w[2] * jy.d[k];
+                float tsum = 0.0f;
 #pragma unroll
-                for (int q = 0; q < 9; q++) t = fmaf(mu[q], f[q].d[k], t);
+                for (int q = 0; q < 9; q++) {
+                    t = fmaf(mu[q], f[q].d[k], t);
+                    tsum += f[q].d[k];
+                }
+                if (p0 + k < 9) t = fmaf(c, rintf(tsum), t);
                 s[p0 + k] = t;
             }
         }

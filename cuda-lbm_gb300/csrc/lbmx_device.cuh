@@ -418,13 +418,15 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
 // the post-collision populations.  The rates (omega, S) and the CM_OPT grid
 // averages have type P: float, or the adjoint's tangent type when gradients
 // with respect to them are wanted.  With OFS, f holds offsets f - w_q on entry
-// and on exit (rho is the full density): the weights' own moments are folded
-// into the equilibrium constants, so 16-bit storage needs no per-population
-// add on load or store.
+// and on exit, and drho = rho - 1 = sum of the offsets comes exactly: every
+// moment is then taken relative to its value at rest (the weights' moments
+// folded in analytically), so the arithmetic keeps FP32 precision in the
+// deviation from rest -- the flow -- and 16-bit storage needs no
+// per-population add on load or store.  Without OFS, drho is unused.
 
 // BGK<2>::apply with Guo forcing -- BGK.cuh:15-39
 template <typename R, bool OFS = false, typename P = float>
-__device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R Fy, P omega, bool forced) {
+__device__ __forceinline__ void collide_bgk(R f[9], R rho, R drho, R ux, R uy, R Fx, R Fy, P omega, bool forced) {
     const R uu = fma(ux, ux, uy * uy);
     const R one = splat(1.0f, ux);
     const R base = fma(splat(-1.5f, ux), uu, one);
@@ -436,10 +438,16 @@ __device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R F
         if (CX(q) == 0) cu = cy * uy;
         else if (CY(q) == 0) cu = cx * ux;
         else cu = fma(cx, ux, cy * uy);
-        // feq = w rho (1 + 3cu + 4.5cu^2 - 1.5uu)
-        const R br = fma(cu, fma(splat(4.5f, ux), cu, splat(3.0f, ux)), base);
-        // offset form: feq - w = (w rho) br - w
-        const R feq = OFS ? fma(WQ(q) * rho, br, splat(-WQ(q), ux)) : (WQ(q) * rho) * br;
+        // feq = w rho (1 + 3cu + 4.5cu^2 - 1.5uu); offset form:
+        // feq - w = w (brm1 + drho (1 + brm1)) with brm1 = br - 1
+        R feq;
+        if (OFS) {
+            const R brm1 = fma(cu, fma(splat(4.5f, ux), cu, splat(3.0f, ux)), splat(-1.5f, ux) * uu);
+            feq = WQ(q) * fma(drho, brm1, brm1 + drho);
+        } else {
+            const R br = fma(cu, fma(splat(4.5f, ux), cu, splat(3.0f, ux)), base);
+            feq = (WQ(q) * rho) * br;
+        }
         R fn = fma(splat(omega, ux), feq - f[q], f[q]);
         if (forced) {
             // w (1 - omega/2) [ (3(c - u) + 9 (c.u) c) . F ]
@@ -456,7 +464,7 @@ __device__ __forceinline__ void collide_bgk(R f[9], R rho, R ux, R uy, R Fx, R F
 // M f_eq of the second-order equilibrium in closed form; the back transform
 // uses M^-1 = M^T diag(1/|row|^2) (the rows are orthogonal).
 template <typename R, bool OFS = false, typename P = float>
-__device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R Fy, const P S[9],
+__device__ __forceinline__ void collide_mrt(R f[9], R rho, R drho, R ux, R uy, R Fx, R Fy, const P S[9],
                                             bool force_quirk, bool forced) {
     const R axis = (f[1] + f[2]) + (f[3] + f[4]);
     const R diag = (f[5] + f[6]) + (f[7] + f[8]);
@@ -476,11 +484,10 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
     const R rux = rho * ux, ruy = rho * uy;
     R meq[9];
     // offset form: m and a are taken relative to the moments of w, (1, -2, 1,
-    // 0, ...): meq[1], meq[2] and a[0] shift by constants, m[1..8] need none
-    meq[1] = OFS ? fma(rho, fma(splat(3.0f, rho), uu, splat(-2.0f, rho)), splat(2.0f, rho))
-                 : rho * fma(splat(3.0f, rho), uu, splat(-2.0f, rho));
-    meq[2] = OFS ? fma(rho, fma(splat(-3.0f, rho), uu, splat(1.0f, rho)), splat(-1.0f, rho))
-                 : rho * fma(splat(-3.0f, rho), uu, splat(1.0f, rho));
+    // 0, ...): meq[1] - (-2) = 3 rho uu - 2 drho, meq[2] - 1 = drho - 3 rho uu,
+    // a[0] = drho / 9; m[1..8] need no shift
+    meq[1] = OFS ? fma(3.0f * rho, uu, -2.0f * drho) : rho * fma(splat(3.0f, rho), uu, splat(-2.0f, rho));
+    meq[2] = OFS ? fma(-3.0f * rho, uu, drho) : rho * fma(splat(-3.0f, rho), uu, splat(1.0f, rho));
     meq[3] = rux;
     meq[4] = -rux;
     meq[5] = ruy;
@@ -492,7 +499,7 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
     const float inv_norm[9] = {1.0f / 9.0f, 1.0f / 36.0f, 1.0f / 36.0f, 1.0f / 6.0f, 1.0f / 12.0f,
                                1.0f / 6.0f, 1.0f / 12.0f, 0.25f, 0.25f};
     R a[9];
-    a[0] = OFS ? fma(splat(1.0f / 9.0f, rho), rho, splat(-1.0f / 9.0f, rho)) : (1.0f / 9.0f) * rho;
+    a[0] = (1.0f / 9.0f) * (OFS ? drho : rho);
 #pragma unroll
     for (int k = 1; k < 9; k++) a[k] = inv_norm[k] * fma(splat(-S[k], rho), m[k] - meq[k], m[k]);
     if (forced) {
@@ -532,85 +539,100 @@ __device__ __forceinline__ void collide_mrt(R f[9], R rho, R ux, R uy, R Fx, R F
 // transform through raw moments (binomial shift) and the raw-moment basis
 // of D2Q9, the same linear map as the reference's closed-form T^-1(u).
 template <typename R, bool OFS = false, typename P = float>
-__device__ __forceinline__ void collide_cm(R f[9], R rho, R ux, R uy, R Fx, R Fy, const P S[9], R hor,
+__device__ __forceinline__ void collide_cm(R f[9], R rho, R drho, R ux, R uy, R Fx, R Fy, const P S[9], R hor,
                                            bool use_hor) {
+    // raw moments; in offset form m20, m02 and m22 are taken relative to their
+    // rest values 1/3, 1/3, 1/9 (the other raw moments vanish at rest)
     const R m10 = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const R m01 = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
-    // offset form: the raw moments of w are m20 = m02 = 1/3, m22 = 1/9
-    const R d22 = (f[5] + f[6]) + (f[7] + f[8]);
-    const R m22 = OFS ? d22 + splat(1.0f / 9.0f, rho) : d22;
-    const R m20 = (f[1] + f[3]) + (OFS ? d22 + splat(1.0f / 3.0f, rho) : d22);
-    const R m02 = (f[2] + f[4]) + (OFS ? d22 + splat(1.0f / 3.0f, rho) : d22);
+    const R m22 = (f[5] + f[6]) + (f[7] + f[8]);
+    const R m20 = (f[1] + f[3]) + m22;
+    const R m02 = (f[2] + f[4]) + m22;
     const R m11 = (f[5] + f[7]) - (f[6] + f[8]);
     const R m21 = (f[5] + f[6]) - (f[7] + f[8]);
     const R m12 = (f[5] + f[8]) - (f[6] + f[7]);
     const R ux2 = ux * ux, uy2 = uy * uy, uxy = ux * uy;
     const R two = splat(2.0f, rho);
-    // central moments kappa_ab = sum f (cx-ux)^a (cy-uy)^b
+    const float third = 1.0f / 3.0f;
+    // central moments kappa_ab = sum f (cx-ux)^a (cy-uy)^b (offset form: k20,
+    // k02 less 1/3 and k22 less 1/9; the rest parts of m20, m02, m22 enter
+    // k21, k12 and k22 as the explicit u/3 terms)
     const R k10 = fma(-ux, rho, m10);
     const R k01 = fma(-uy, rho, m01);
     const R k20 = fma(ux2, rho, fma(-two * ux, m10, m20));
     const R k02 = fma(uy2, rho, fma(-two * uy, m01, m02));
     const R k11 = fma(uxy, rho, fma(-ux, m01, fma(-uy, m10, m11)));
-    const R k21 = fma(-(ux2 * uy), rho, fma(two * uxy, m10, fma(ux2, m01, fma(-uy, m20, fma(-two * ux, m11, m21)))));
-    const R k12 = fma(-(ux * uy2), rho, fma(two * uxy, m01, fma(uy2, m10, fma(-ux, m02, fma(-two * uy, m11, m12)))));
-    const R k22 = fma(ux2 * uy2, rho,
-                      fma(-two * (ux2 * uy), m01,
-                          fma(-two * (ux * uy2), m10,
-                              fma(splat(4.0f, rho) * uxy, m11,
-                                  fma(uy2, m20, fma(ux2, m02, fma(-two * uy, m21, fma(-two * ux, m12, m22))))))));
+    R k21 = fma(-(ux2 * uy), rho, fma(two * uxy, m10, fma(ux2, m01, fma(-uy, m20, fma(-two * ux, m11, m21)))));
+    R k12 = fma(-(ux * uy2), rho, fma(two * uxy, m01, fma(uy2, m10, fma(-ux, m02, fma(-two * uy, m11, m12)))));
+    R k22 = fma(ux2 * uy2, rho,
+                fma(-two * (ux2 * uy), m01,
+                    fma(-two * (ux * uy2), m10,
+                        fma(splat(4.0f, rho) * uxy, m11,
+                            fma(uy2, m20, fma(ux2, m02, fma(-two * uy, m21, fma(-two * ux, m12, m22))))))));
+    if (OFS) {
+        k21 = fma(-uy, splat(third, rho), k21);
+        k12 = fma(-ux, splat(third, rho), k12);
+        k22 = fma(ux2 + uy2, splat(third, rho), k22);
+    }
     const float cs2 = 1.0f / 3.0f;
     // relaxation k - s (k - k_eq) + (1 - s/2) F with k_eq = [rho, 0, 0,
     // 2 rho cs2, 0, 0, 0, 0, rho cs2^2] and F = [0, Fx, Fy, 0, 0, 0, Fy cs2, Fx cs2, 0]
+    // (offset form: k_eq of ksum and k22 less their rest values, in drho)
     const R s3 = splat(S[3], rho), s4 = splat(S[4], rho), s5 = splat(S[5], rho);
     const R s6 = use_hor ? hor : splat(S[6], rho);
     const R s7 = use_hor ? hor : splat(S[7], rho);
     const R s8 = use_hor ? hor : splat(S[8], rho);
     const R one = splat(1.0f, rho), half = splat(0.5f, rho);
+    const R rr = OFS ? drho : rho;
     const R c10 = fma(splat(-S[1], rho), k10, k10) + (1.0f - 0.5f * S[1]) * Fx;
     const R c01 = fma(splat(-S[2], rho), k01, k01) + (1.0f - 0.5f * S[2]) * Fy;
     const R ksum = k20 + k02, kdiff = k20 - k02;
-    const R t3 = fma(-s3, ksum - (2.0f * cs2) * rho, ksum);
+    const R t3 = fma(-s3, ksum - (2.0f * cs2) * rr, ksum);
     const R t4 = fma(-s4, kdiff, kdiff);
     const R c11 = fma(-s5, k11, k11);
     const R c21 = fma(fma(-half, s6, one), cs2 * Fy, fma(-s6, k21, k21));
     const R c12 = fma(fma(-half, s7, one), cs2 * Fx, fma(-s7, k12, k12));
-    const R c22 = fma(-s8, k22 - (cs2 * cs2) * rho, k22);
+    const R c22 = fma(-s8, k22 - (cs2 * cs2) * rr, k22);
     const R c20 = 0.5f * (t3 + t4), c02 = 0.5f * (t3 - t4);
     const R c00 = rho;
     // back to raw moments (binomial shift by +u), then to populations
-    // (offset form: minus the raw moments of w, 1, 1/3, 1/3, 1/9)
+    // (offset form: r20, r02, r22 less their rest values; c20, c02 carry the
+    // 1/3 into r21 and r12 explicitly)
     const R r10 = fma(ux, c00, c10);
     const R r01 = fma(uy, c00, c01);
     const R r20 = fma(ux2, c00, fma(two * ux, c10, c20));
     const R r02 = fma(uy2, c00, fma(two * uy, c01, c02));
     const R r11 = fma(uxy, c00, fma(ux, c01, fma(uy, c10, c11)));
-    const R r21 = fma(ux2 * uy, c00, fma(two * uxy, c10, fma(ux2, c01, fma(uy, c20, fma(two * ux, c11, c21)))));
-    const R r12 = fma(ux * uy2, c00, fma(two * uxy, c01, fma(uy2, c10, fma(ux, c02, fma(two * uy, c11, c12)))));
-    const R r22 = fma(ux2 * uy2, c00,
-                      fma(two * (ux2 * uy), c01,
-                          fma(two * (ux * uy2), c10,
-                              fma(splat(4.0f, rho) * uxy, c11,
-                                  fma(uy2, c20, fma(ux2, c02, fma(two * uy, c21, fma(two * ux, c12, c22))))))));
-    const R o00 = OFS ? c00 - splat(1.0f, rho) : c00;
-    const R o20 = OFS ? r20 - splat(1.0f / 3.0f, rho) : r20;
-    const R o02 = OFS ? r02 - splat(1.0f / 3.0f, rho) : r02;
-    const R o22 = OFS ? r22 - splat(1.0f / 9.0f, rho) : r22;
-    f[0] = (o00 - (o20 + o02)) + o22;
-    f[1] = 0.5f * ((r10 + o20) - (r12 + o22));
-    f[3] = 0.5f * ((o20 + r12) - (r10 + o22));
-    f[2] = 0.5f * ((r01 + o02) - (r21 + o22));
-    f[4] = 0.5f * ((o02 + r21) - (r01 + o22));
-    f[5] = 0.25f * ((r11 + r21) + (r12 + o22));
-    f[6] = 0.25f * ((r21 + o22) - (r11 + r12));
-    f[7] = 0.25f * ((r11 + o22) - (r21 + r12));
-    f[8] = 0.25f * ((r12 + o22) - (r11 + r21));
+    R r21 = fma(ux2 * uy, c00, fma(two * uxy, c10, fma(ux2, c01, fma(uy, c20, fma(two * ux, c11, c21)))));
+    R r12 = fma(ux * uy2, c00, fma(two * uxy, c01, fma(uy2, c10, fma(ux, c02, fma(two * uy, c11, c12)))));
+    R r22 = fma(ux2 * uy2, c00,
+                fma(two * (ux2 * uy), c01,
+                    fma(two * (ux * uy2), c10,
+                        fma(splat(4.0f, rho) * uxy, c11,
+                            fma(uy2, c20, fma(ux2, c02, fma(two * uy, c21, fma(two * ux, c12, c22))))))));
+    if (OFS) {
+        r21 = fma(uy, splat(third, rho), r21);
+        r12 = fma(ux, splat(third, rho), r12);
+        r22 = fma(ux2 + uy2, splat(third, rho), r22);
+    }
+    const R o00 = OFS ? drho : c00;
+    f[0] = (o00 - (r20 + r02)) + r22;
+    f[1] = 0.5f * ((r10 + r20) - (r12 + r22));
+    f[3] = 0.5f * ((r20 + r12) - (r10 + r22));
+    f[2] = 0.5f * ((r01 + r02) - (r21 + r22));
+    f[4] = 0.5f * ((r02 + r21) - (r01 + r22));
+    f[5] = 0.25f * ((r11 + r21) + (r12 + r22));
+    f[6] = 0.25f * ((r21 + r22) - (r11 + r12));
+    f[7] = 0.25f * ((r11 + r22) - (r21 + r12));
+    f[8] = 0.25f * ((r12 + r22) - (r11 + r21));
 }
 
 // Initial populations f_eq(rho, u) (init_node, src/core/init/init.cuh:12-27):
 // second-order equilibrium, bracket in double as equilibrium.cu:13-38
 // evaluates it (cs^2 and cs^4 rounded to float first, as there); the
-// divisions become products with the reciprocals, computed once.
+// divisions become products with the reciprocals, computed once.  OFS: the
+// offsets f_eq - w_q, formed in double before the rounding.
+template <bool OFS = false>
 __device__ __forceinline__ void init_equilibrium(float rho, float ux, float uy, float fe[9]) {
     const float cs = 1.0f / sqrtf(3.0f);
     const float cs2 = cs * cs, cs4 = cs2 * cs2;
@@ -621,7 +643,7 @@ __device__ __forceinline__ void init_equilibrium(float rho, float ux, float uy, 
     for (int q = 0; q < 9; q++) {
         const double cu = (double)((float)CX(q) * ux + (float)CY(q) * uy);
         const double br = base + cu * cu * half_inv_cs4 + cu * inv_cs2;
-        fe[q] = (float)((double)(WQ(q) * rho) * br);
+        fe[q] = OFS ? (float)((double)(WQ(q) * rho) * br - (double)WQ(q)) : (float)((double)(WQ(q) * rho) * br);
     }
 }
 

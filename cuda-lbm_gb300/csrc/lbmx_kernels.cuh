@@ -154,14 +154,14 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, doubl
     }
     if (a.check_finite && !isfinite(rho)) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {
-        collide_bgk<float>(f, rho, ux, uy, Fx, Fy, a.omega, a.forced);
+        collide_bgk<float>(f, rho, rho, ux, uy, Fx, Fy, a.omega, a.forced);
     } else if (OP == LBMX_MRT) {
-        collide_mrt<float>(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
+        collide_mrt<float>(f, rho, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
     } else if (OP == LBMX_CM) {
-        collide_cm<float>(f, rho, ux, uy, Fx, Fy, a.S, 0.f, false);
+        collide_cm<float>(f, rho, rho, ux, uy, Fx, Fy, a.S, 0.f, false);
     } else {
         const float jmag = sqrtf(ux * ux + uy * uy) * rho;
-        collide_cm<float>(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate<float>(rho, jmag, pimag, a.avg), true);
+        collide_cm<float>(f, rho, rho, ux, uy, Fx, Fy, a.S, optimal_rate<float>(rho, jmag, pimag, a.avg), true);
     }
     store_post_collision<T>(a, x, y, f, outmask, fl);
 }
@@ -298,6 +298,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         else f[q].v = Store<T>::ld2r(s);
     }
     V2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
+    const V2 drho = rho;                     // offset form: rho - 1, exactly
     if (OFS) rho = rho + splat(1.0f, rho);  // the weights sum to 1
     const V2 jx = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const V2 jy = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
@@ -333,14 +334,14 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     }
     if (a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {
-        collide_bgk<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.omega, a.forced);
+        collide_bgk<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.omega, a.forced);
     } else if (OP == LBMX_MRT) {
-        collide_mrt<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
+        collide_mrt<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, a.forced);
     } else if (OP == LBMX_CM) {
-        collide_cm<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.S, rho, false);
+        collide_cm<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.S, rho, false);
     } else {
         const V2 jmag = rho * vsqrt(fma(ux, ux, uy * uy));
-        collide_cm<V2, OFS>(f, rho, ux, uy, Fx, Fy, a.S, optimal_rate<V2>(rho, jmag, pimag, a.avg), true);
+        collide_cm<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.S, optimal_rate<V2>(rho, jmag, pimag, a.avg), true);
     }
     Store<T>::st2r(F + a.rest_plane * plane + off, f[0].v);
 #pragma unroll

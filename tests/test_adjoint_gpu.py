@@ -89,7 +89,9 @@ def test_adjoint_forward_matches_engine_and_oracle(op):
     ro, uo, _ = o.moments()
     assert np.abs(ra - ro).max() < 2e-5 and np.abs(ua - uo).max() < 2e-5
     fx = float(c["force"][0].flat[0])
-    assert rel(J, oracle_J(c, c["gamma"].astype(np.float64), c["omega"], fx, 0.0)) < 1e-5
+    # FP32 vs FP64 of a drag-damped flow: the flux has fallen to ~1% of its
+    # start, so the bound is relative to the starting flux (~0.66)
+    assert abs(J - oracle_J(c, c["gamma"].astype(np.float64), c["omega"], fx, 0.0)) < 1e-6
     # the engine's production step on the same case (20 steps: CM_OPT's
     # clamped rate lets rounding differences of the two paths grow later)
     a20 = make_adjoint(c)
