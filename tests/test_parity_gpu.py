@@ -198,6 +198,30 @@ def test_staged_tiles_many_per_cta(case, steps):
     compare(o, L)
 
 
+@pytest.mark.parametrize("op", [C.BGK, C.MRT, C.CM, C.CM_OPT])
+def test_brinkman_drag(op):
+    # per-node Brinkman field (no reference counterpart) against the oracle's
+    # restatement of the same term; CM_OPT over a short horizon (its clamped
+    # rate amplifies rounding once the drag has slowed the flow)
+    c = C.channel_brinkman(96, 40, op=op, sigma=3.0, gamma_scale=0.3 if op != C.CM_OPT else 0.02)
+    c["u"] = c["u"] + 0.02 * np.random.default_rng(3).standard_normal(c["u"].shape)
+    o = C.make_oracle(c)
+    o.set_gamma(c["gamma"])
+    L = C.make_lattice(c)
+    L.set_brinkman(c["gamma"])
+    steps = 20 if op == C.CM_OPT else 60
+    o.step(steps)
+    L.step(steps)
+    compare(o, L)
+    # and gamma = 0 is the plain step, bit for bit
+    L0 = C.make_lattice(c)
+    L0.set_brinkman(np.zeros_like(c["gamma"]))
+    L1 = C.make_lattice(c)
+    L0.step(7)
+    L1.step(7)
+    np.testing.assert_array_equal(L0.moments()[1], L1.moments()[1])
+
+
 @pytest.mark.parametrize("storage,tol", [(1, 5e-4), (2, 4e-3)])
 def test_offset_storage_against_fp32(storage, tol):
     c = C.cavity_moving_wall(96, 96, op=C.MRT, nu=0.05)
