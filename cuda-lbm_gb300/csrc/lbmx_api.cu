@@ -191,6 +191,17 @@ static lbmx_status check_pipeline(lbmx_handle* h) {
 void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.parity = (int)(s & 1);
     a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? (a.parity ? 9 : 0) : 0;
+    // interior store targets: parity 1 -> slot q of the node x + c_q,
+    // parity 0 -> the node's own slot OPP(q) (D2Q9 order: rest, E, N, W, S, NE, NW, SW, SE)
+    static const int cx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    static const int cy[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    static const int opp[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+    const long long es = (long long)elem_size(h->p.storage);
+    const Geometry& g = h->g;
+    a.st_off[0] = (long long)a.rest_plane * g.plane * es;
+    for (int q = 1; q < 9; q++)
+        a.st_off[q] = (a.parity ? (long long)q * g.plane + (long long)cy[q] * g.pitch + cx[q]
+                                : (long long)opp[q] * g.plane) * es;
 }
 
 static void free_ibm(lbmx_handle* h) {

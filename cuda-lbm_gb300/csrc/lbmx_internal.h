@@ -47,6 +47,8 @@ struct StepArgs {
     uint32_t quirks;
     int parity;              // step index & 1; 1 = neighbour-access phase
     int rest_plane;          // plane that holds f0 this step (0 or 9)
+    long long st_off[9];     // byte offset, from a node's plane-0 element, of the slot its q-th
+                             // post-collision population goes to this step (interior nodes)
     float omega;
     float S[9];
     float u_bc, wall_ux, wall_uy, rho_out_bc;

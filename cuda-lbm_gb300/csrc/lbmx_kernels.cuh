@@ -277,7 +277,9 @@ __device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap
 }
 
 // Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
-template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH>
+// LEAN: no per-node force or Brinkman field, no moment store, no sums, no
+// finite check (chosen at launch), so the unit is straight-line code.
+template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, bool LEAN = false>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
                                               double v[6]) {
     using St = Staging<T, TW, TH>;
@@ -303,28 +305,28 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     const V2 jx = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const V2 jy = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
     V2 Fx = {make_float2(a.body_fx, a.body_fx)}, Fy = {make_float2(a.body_fy, a.body_fy)};
-    if (a.force) {
+    if (!LEAN && a.force) {
         Fx.v = *reinterpret_cast<const float2*>(a.force + off);
         Fy.v = *reinterpret_cast<const float2*>(a.force + plane + off);
     }
     const V2 inv = vdiv(splat(1.0f, rho), rho);
     V2 ux = fma(0.5f * Fx, inv, jx * inv);
     V2 uy = fma(0.5f * Fy, inv, jy * inv);
-    if (a.gamma) brinkman<V2>(V2{*reinterpret_cast<const float2*>(a.gamma + off)}, rho, ux, uy, Fx, Fy);
+    if (!LEAN && a.gamma) brinkman<V2>(V2{*reinterpret_cast<const float2*>(a.gamma + off)}, rho, ux, uy, Fx, Fy);
     V2 pimag = splat(0.f, rho);
-    if (OP == LBMX_CM_OPT || a.partials) {
+    if (OP == LBMX_CM_OPT || (!LEAN && a.partials)) {
         // offset form: sum c_x^2 w = sum c_y^2 w = 1/3
         const V2 d = OFS ? (f[5] + f[6]) + ((f[7] + f[8]) + splat(1.0f / 3.0f, rho)) : (f[5] + f[6]) + (f[7] + f[8]);
         const V2 pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
         const V2 pxy = (f[5] + f[7]) - (f[6] + f[8]);
         pimag = vsqrt(fma(pxx, pxx, fma(2.0f * pxy, pxy, pyy * pyy)));
     }
-    if (a.rho_out) {
+    if (!LEAN && a.rho_out) {
         *reinterpret_cast<float2*>(a.rho_out + off) = rho.v;
         *reinterpret_cast<float2*>(a.u_out + off) = ux.v;
         *reinterpret_cast<float2*>(a.u_out + plane + off) = uy.v;
     }
-    if (a.partials) {
+    if (!LEAN && a.partials) {
         v[0] += (double)rho.v.x + (double)rho.v.y;
         v[1] += (double)rho.v.x * ux.v.x + (double)rho.v.y * ux.v.y;
         v[2] += (double)rho.v.x * uy.v.x + (double)rho.v.y * uy.v.y;
@@ -332,7 +334,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         v[4] += rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x) + rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y);
         v[5] += (double)pimag.v.x + (double)pimag.v.y;
     }
-    if (a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
+    if (!LEAN && a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {
         collide_bgk<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.omega, a.forced);
     } else if (OP == LBMX_MRT) {
@@ -343,20 +345,17 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         const V2 jmag = rho * vsqrt(fma(ux, ux, uy * uy));
         collide_cm<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.S, optimal_rate<V2>(rho, jmag, pimag, a.avg), true);
     }
-    Store<T>::st2r(F + a.rest_plane * plane + off, f[0].v);
+    // slot q of the downstream nodes x + c_q (parity 1) or the nodes' own
+    // slot OPP(q) (parity 0): byte offsets of this launch, from the host
+    char* base = reinterpret_cast<char*>(F + off);
 #pragma unroll
-    for (int q = 1; q < 9; q++) {
-        if (P == 0) {
-            Store<T>::st2r(F + OPP(q) * plane + off, f[q].v);  // own slot OPP(q)
+    for (int q = 0; q < 9; q++) {
+        T* p = reinterpret_cast<T*>(base + a.st_off[q]);
+        if (P == 0 || CX(q) == 0) {
+            Store<T>::st2r(p, f[q].v);
         } else {
-            // slot q of the downstream nodes x + c_q
-            T* p = F + q * plane + off + (long long)CY(q) * pitch + CX(q);
-            if (CX(q) == 0) {
-                Store<T>::st2r(p, f[q].v);
-            } else {
-                Store<T>::str(p, f[q].v.x);
-                Store<T>::str(p + 1, f[q].v.y);
-            }
+            Store<T>::str(p, f[q].v.x);
+            Store<T>::str(p + 1, f[q].v.y);
         }
     }
 }
@@ -372,7 +371,7 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
     if (x < a.g.nx) general_node<T, OP>(a, x, y, v);
 }
 
-template <typename T, int OP, int P>
+template <typename T, int OP, int P, bool LEAN>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
     // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
     // work item from a global counter; for an interior tile it bulk-copies
@@ -473,7 +472,9 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                     const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
                     live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
                 }
-                if (live) interior_unit<T, OP, P>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
+                if (live)
+                    interior_unit<T, OP, P, kStageW, kStageH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0,
+                                                                     y, v);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);
@@ -676,28 +677,35 @@ __global__ void ibm_gather_kernel(const StepArgs a, const int* patch_nodes, int 
     pu[npatch + i] = jy * inv;
 }
 
-template <typename T, int OP, int P>
+template <typename T, int OP, int P, bool LEAN>
 static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tmap, unsigned grid, cudaStream_t s) {
     // the staged ring needs more than the default 48 KB; set once per device
     static unsigned long long configured = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     if (!(configured >> (dev & 63) & 1ull)) {
-        cudaError_t e = cudaFuncSetAttribute(step_kernel<T, OP, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Staging<T>::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(step_kernel<T, OP, P, LEAN>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Staging<T>::SMEM);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    step_kernel<T, OP, P><<<grid, kThreads, Staging<T>::SMEM, s>>>(a, tmap);
+    step_kernel<T, OP, P, LEAN><<<grid, kThreads, Staging<T>::SMEM, s>>>(a, tmap);
     return cudaGetLastError();
+}
+
+template <typename T, int OP, int P>
+static cudaError_t launch_step_lean(const StepArgs& a, const CUtensorMap& tmap, unsigned grid, cudaStream_t s) {
+    const bool lean = !a.force && !a.gamma && !a.rho_out && !a.partials && !a.check_finite;
+    return lean ? launch_step_variant<T, OP, P, true>(a, tmap, grid, s)
+                : launch_step_variant<T, OP, P, false>(a, tmap, grid, s);
 }
 
 template <typename T>
 cudaError_t launch_step(const StepArgs& a, const CUtensorMap& tmap, int op, cudaStream_t s) {
     const unsigned grid = (unsigned)a.num_ctas;
 #define LBMX_STEP_CASE(OPV)                                                    \
-    return a.parity ? launch_step_variant<T, OPV, 1>(a, tmap, grid, s)         \
-                    : launch_step_variant<T, OPV, 0>(a, tmap, grid, s);
+    return a.parity ? launch_step_lean<T, OPV, 1>(a, tmap, grid, s)            \
+                    : launch_step_lean<T, OPV, 0>(a, tmap, grid, s);
     switch (op) {
     case LBMX_BGK: LBMX_STEP_CASE(LBMX_BGK)
     case LBMX_MRT: LBMX_STEP_CASE(LBMX_MRT)
