@@ -152,8 +152,9 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     }
     h->nspecial = (int)units.size();
     h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
-    h->tiles_x = (g.nx + kStageW - 1) / kStageW;
-    h->tiles_y = (g.ny - 2 + kStageH - 1) / kStageH;
+    const int es = (int)elem_size(h->p.storage);
+    h->tiles_x = (g.nx + step_tile_w(es) - 1) / step_tile_w(es);
+    h->tiles_y = (g.ny - 2 + step_tile_h(es) - 1) / step_tile_h(es);
     // persistent CTAs walk the work list: kCtasPerSm per SM on large
     // lattices; two per SM when each CTA would get fewer than 16 items (a
     // small lattice is latency-bound and gains more from fuller CTAs than
@@ -289,7 +290,8 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     h->f = static_cast<char*>(h->f_alloc) + (size_t)kGuardElems * elem_size(p->storage);
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (h->num_sms < 1) h->num_sms = 1;
-    if (!encode_population_map(h, &h->tmap, kStageW, kStageH)) {
+    if (!encode_population_map(h, &h->tmap, step_tile_w((int)elem_size(p->storage)),
+                               step_tile_h((int)elem_size(p->storage)))) {
         fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: cannot build the TMA descriptor (cuTensorMapEncodeTiled)");
         lbmx_destroy(h);
         return LBMX_ERR_CUDA;

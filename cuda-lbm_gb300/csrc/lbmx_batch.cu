@@ -37,6 +37,7 @@ struct lbmx_batch {
     unsigned int* error_word = nullptr;
     std::vector<StepArgs> host_args;   // what d_args holds
     int args_tile_w = 0, args_tile_h = 0;  // tile shape d_tmaps / d_items were built for
+    bool lean = false;                     // no lattice has a per-node force or Brinkman field
     // streams of the lattices (distinct), one event each, and the batch's end event
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> stream_events;
@@ -152,6 +153,8 @@ static lbmx_status refresh(lbmx_batch* b) {
     b->host_args.swap(args);
     b->args_tile_w = tw;
     b->args_tile_h = th;
+    b->lean = true;
+    for (const lbmx_handle* h : b->lat) b->lean = b->lean && !h->force && !h->gamma;
     return LBMX_OK;
 }
 
@@ -179,9 +182,12 @@ static lbmx_status launch_one(lbmx_batch* b, long long s, int variant) {
     ba.done = b->done;
     ba.error_word = b->error_word;
     const unsigned grid = (unsigned)std::max(1, std::min(b->nitems, b->cfg.ctas_per_sm * b->num_sms));
+    // plain steps of lattices without per-node force or Brinkman fields run
+    // the kernel without those branches
+    const bool lean = variant == 0 && b->lean;
     BATCH_CUDA(b, dispatch(b->storage, [&](auto tag) {
-                   return launch_batch_step<decltype(tag)>(ba, b->op, parity, b->cfg.tile_w, b->cfg.tile_h, grid,
-                                                           b->stream);
+                   return launch_batch_step<decltype(tag)>(ba, b->op, parity, b->cfg.tile_w, b->cfg.tile_h, lean,
+                                                           grid, b->stream);
                }));
     return LBMX_OK;
 }
@@ -189,9 +195,15 @@ static lbmx_status launch_one(lbmx_batch* b, long long s, int variant) {
 // CUDA graphs of graph_steps plain steps, one per parity of the first step.
 static lbmx_status build_graphs(lbmx_batch* b) {
     const int len = b->cfg.graph_steps;
+    // the kernels' shared-memory attributes are set outside the capture
+    BatchArgs none;
+    memset(&none, 0, sizeof(none));
+    for (int p = 0; p < 2; p++)
+        BATCH_CUDA(b, dispatch(b->storage, [&](auto tag) {
+                       return launch_batch_step<decltype(tag)>(none, b->op, p, b->cfg.tile_w, b->cfg.tile_h, b->lean, 0,
+                                                               b->stream);
+                   }));
     for (int p = 0; p < 2; p++) {
-        // attribute setup outside the capture: one direct launch of each parity
-        // has run before any graph is built (see lbmx_batch_step)
         cudaGraph_t g = nullptr;
         BATCH_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         lbmx_status st = LBMX_OK;
@@ -211,13 +223,11 @@ static lbmx_status build_graphs(lbmx_batch* b) {
 }
 
 // nsteps steps from step count t; last_variant for the final step.
-static lbmx_status run_steps(lbmx_batch* b, long long t, int nsteps, int last_variant, bool* primed) {
+static lbmx_status run_steps(lbmx_batch* b, long long t, int nsteps, int last_variant) {
     int i = 0;
-    // the first two steps of every call run directly: they set up the kernels'
-    // attributes before any capture
     while (i < nsteps) {
         const int left = nsteps - i;
-        const bool graphable = b->cfg.graph_steps > 0 && *primed && left - 1 >= b->cfg.graph_steps;
+        const bool graphable = b->cfg.graph_steps > 0 && left - 1 >= b->cfg.graph_steps;
         if (graphable) {
             if (b->graph_len != b->cfg.graph_steps) {
                 drop_graphs(b);
@@ -231,7 +241,6 @@ static lbmx_status run_steps(lbmx_batch* b, long long t, int nsteps, int last_va
         lbmx_status st = launch_one(b, t + i + 1, i == nsteps - 1 ? last_variant : 0);
         if (st != LBMX_OK) return st;
         i++;
-        if (i >= 2) *primed = true;
     }
     return LBMX_OK;
 }
@@ -386,8 +395,7 @@ lbmx_status lbmx_batch_step(lbmx_batch* b, int32_t nsteps, uint32_t flags) {
     const long long t = b->lat[0]->t;
     if ((st = wait_lattices(b)) != LBMX_OK) return st;
     if (check) BATCH_CUDA(b, cudaMemsetAsync(b->error_word, 0, sizeof(unsigned int), b->stream));
-    bool primed = b->graph_len == b->cfg.graph_steps && b->graph[0] != nullptr;
-    st = run_steps(b, t, nsteps, last, &primed);
+    st = run_steps(b, t, nsteps, last);
     if (st != LBMX_OK) return st;
     for (lbmx_handle* h : b->lat) h->t = t + nsteps;
     if ((st = release_lattices(b)) != LBMX_OK) return st;
@@ -465,21 +473,20 @@ lbmx_status lbmx_batch_autotune(lbmx_batch* b, int32_t trial_steps, lbmx_batch_c
     long long t = t0;
     st = LBMX_OK;
     static const int shapes[3][2] = {{64, 8}, {128, 4}, {128, 8}};
-    static const int chunks[3] = {1, 2, 4};
+    static const int chunks[5] = {1, 2, 4, 8, 16};
     for (int ti = 0; ti < 3 && st == LBMX_OK; ti++)
         for (int c = 1; c <= kCtasPerSm && st == LBMX_OK; c++)
-            for (int ki = 0; ki < 3 && st == LBMX_OK; ki++) {
+            for (int ki = 0; ki < 5 && st == LBMX_OK; ki++) {
                 // trials launch directly: one launch per step for every
                 // candidate, so graphs would not change the ranking
                 lbmx_batch_config cand{shapes[ti][0], shapes[ti][1], c, chunks[ki], 0};
                 b->cfg = cand;
                 drop_graphs(b);
                 if ((st = refresh(b)) != LBMX_OK) break;
-                bool primed = false;
-                if ((st = run_steps(b, t, 2, 0, &primed)) != LBMX_OK) break;
+                if ((st = run_steps(b, t, 2, 0)) != LBMX_OK) break;
                 t += 2;
                 if (cudaEventRecord(e0, b->stream) != cudaSuccess) { st = LBMX_ERR_CUDA; break; }
-                if ((st = run_steps(b, t, trial_steps, 0, &primed)) != LBMX_OK) break;
+                if ((st = run_steps(b, t, trial_steps, 0)) != LBMX_OK) break;
                 t += trial_steps;
                 if (cudaEventRecord(e1, b->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
                     st = bfail(b, LBMX_ERR_CUDA, "lbmx_batch_autotune: trial failed");

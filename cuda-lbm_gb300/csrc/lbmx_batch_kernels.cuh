@@ -18,8 +18,9 @@
 
 namespace lbmx {
 
-template <typename T, int OP, int P, int TW, int TH>
-__global__ void __launch_bounds__(kThreads, (TW * TH > kStageW * kStageH) ? 2 : kCtasPerSm) batch_step_kernel(const BatchArgs b) {
+template <typename T, int OP, int P, int TW, int TH, bool LEAN>
+__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW * kStageH) ? 2 : kCtasPerSm)
+    batch_step_kernel(const BatchArgs b) {
     using St = Staging<T, TW, TH>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* bufs = reinterpret_cast<T*>(smem_raw);
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(kThreads, (TW * TH > kStageW * kStageH) ? 2 : 
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
                     }
                     if (live)
-                        interior_unit<T, OP, P, TW, TH>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
+                        interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
                 }
             } else {
                 special_chunk<T, OP>(a, -2 - sl.x, tid, v);
@@ -128,50 +129,53 @@ __global__ void __launch_bounds__(kThreads, (TW * TH > kStageW * kStageH) ? 2 : 
 }
 
 // grid == 0: only set the kernel's shared-memory attribute (before a capture)
-template <typename T, int OP, int P, int TW, int TH>
+template <typename T, int OP, int P, int TW, int TH, bool LEAN>
 static cudaError_t launch_batch_variant(const BatchArgs& b, unsigned grid, cudaStream_t s) {
     static unsigned long long configured = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     if (!(configured >> (dev & 63) & 1ull)) {
-        cudaError_t e = cudaFuncSetAttribute(batch_step_kernel<T, OP, P, TW, TH>,
+        cudaError_t e = cudaFuncSetAttribute(batch_step_kernel<T, OP, P, TW, TH, LEAN>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Staging<T, TW, TH>::SMEM);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
     if (grid == 0) return cudaSuccess;
-    batch_step_kernel<T, OP, P, TW, TH><<<grid, kThreads, Staging<T, TW, TH>::SMEM, s>>>(b);
+    batch_step_kernel<T, OP, P, TW, TH, LEAN><<<grid, kThreads, Staging<T, TW, TH>::SMEM, s>>>(b);
     return cudaGetLastError();
 }
 
 template <typename T, int OP, int TW, int TH>
-static cudaError_t launch_batch_shape(const BatchArgs& b, int parity, unsigned grid, cudaStream_t s) {
-    return parity ? launch_batch_variant<T, OP, 1, TW, TH>(b, grid, s)
-                  : launch_batch_variant<T, OP, 0, TW, TH>(b, grid, s);
+static cudaError_t launch_batch_shape(const BatchArgs& b, int parity, bool lean, unsigned grid, cudaStream_t s) {
+    if (lean)
+        return parity ? launch_batch_variant<T, OP, 1, TW, TH, true>(b, grid, s)
+                      : launch_batch_variant<T, OP, 0, TW, TH, true>(b, grid, s);
+    return parity ? launch_batch_variant<T, OP, 1, TW, TH, false>(b, grid, s)
+                  : launch_batch_variant<T, OP, 0, TW, TH, false>(b, grid, s);
 }
 
 template <typename T, int OP>
-static cudaError_t launch_batch_op(const BatchArgs& b, int parity, int tile_w, int tile_h, unsigned grid,
+static cudaError_t launch_batch_op(const BatchArgs& b, int parity, int tile_w, int tile_h, bool lean, unsigned grid,
                                    cudaStream_t s) {
-    if (tile_w == 64 && tile_h == 8) return launch_batch_shape<T, OP, 64, 8>(b, parity, grid, s);
-    if (tile_w == 128 && tile_h == 4) return launch_batch_shape<T, OP, 128, 4>(b, parity, grid, s);
-    if (tile_w == 128 && tile_h == 8) return launch_batch_shape<T, OP, 128, 8>(b, parity, grid, s);
+    if (tile_w == 64 && tile_h == 8) return launch_batch_shape<T, OP, 64, 8>(b, parity, lean, grid, s);
+    if (tile_w == 128 && tile_h == 4) return launch_batch_shape<T, OP, 128, 4>(b, parity, lean, grid, s);
+    if (tile_w == 128 && tile_h == 8) return launch_batch_shape<T, OP, 128, 8>(b, parity, lean, grid, s);
     return cudaErrorInvalidValue;
 }
 
 template <typename T>
-cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w, int tile_h, unsigned grid,
-                              cudaStream_t s) {
+cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w, int tile_h, bool lean,
+                              unsigned grid, cudaStream_t s) {
     switch (op) {
-    case LBMX_BGK: return launch_batch_op<T, LBMX_BGK>(b, parity, tile_w, tile_h, grid, s);
-    case LBMX_MRT: return launch_batch_op<T, LBMX_MRT>(b, parity, tile_w, tile_h, grid, s);
-    case LBMX_CM: return launch_batch_op<T, LBMX_CM>(b, parity, tile_w, tile_h, grid, s);
+    case LBMX_BGK: return launch_batch_op<T, LBMX_BGK>(b, parity, tile_w, tile_h, lean, grid, s);
+    case LBMX_MRT: return launch_batch_op<T, LBMX_MRT>(b, parity, tile_w, tile_h, lean, grid, s);
+    case LBMX_CM: return launch_batch_op<T, LBMX_CM>(b, parity, tile_w, tile_h, lean, grid, s);
     default: return cudaErrorInvalidValue;
     }
 }
 
 #define LBMX_INSTANTIATE_BATCH(T) \
-    template cudaError_t launch_batch_step<T>(const BatchArgs&, int, int, int, int, unsigned, cudaStream_t);
+    template cudaError_t launch_batch_step<T>(const BatchArgs&, int, int, int, int, bool, unsigned, cudaStream_t);
 
 }  // namespace lbmx

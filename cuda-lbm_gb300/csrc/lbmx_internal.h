@@ -125,8 +125,8 @@ struct BatchArgs {
 // tile shape tile_w x tile_h: 64 x 8, 128 x 4 or 128 x 8; op: BGK, MRT or CM;
 // grid 0 only prepares the kernel (attributes) for a later graph capture
 template <typename T>
-cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w, int tile_h, unsigned grid,
-                              cudaStream_t s);
+cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w, int tile_h, bool lean,
+                              unsigned grid, cudaStream_t s);
 
 // step-kernel geometry: an interior tile is 128 x 4 nodes; each of the 256
 // consumer threads takes two x-neighbouring nodes of one row.  The batched
@@ -136,6 +136,25 @@ constexpr int kConsumerWarps = 8;
 constexpr int kCtasPerSm = 3;      // resident persistent CTAs per SM (72 registers per thread)
 constexpr int kStageW = 128;
 constexpr int kStageH = 4;
+// The single-lattice kernel's tile shape for 16-bit storage, and the ring
+// depth of 16-bit tiles larger than 512 nodes.  128 x 8 tiles, two units per
+// consumer thread in a 3-stage ring, measured fastest on GB300 for 16-bit
+// storage (issue-bound there: the per-tile work is spread over two units).
+#ifndef LBMX_TW16
+#define LBMX_TW16 128
+#endif
+#ifndef LBMX_TH16
+#define LBMX_TH16 8
+#endif
+#ifndef LBMX_NST16
+#define LBMX_NST16 3
+#endif
+constexpr int kStageW16 = LBMX_TW16;
+constexpr int kStageH16 = LBMX_TH16;
+// interior tile shape of the single-lattice step kernel, by element size
+// (a tile of more than 512 nodes gives each consumer thread several units)
+__host__ __device__ constexpr int step_tile_w(int elem_bytes) { return elem_bytes == 2 ? kStageW16 : kStageW; }
+__host__ __device__ constexpr int step_tile_h(int elem_bytes) { return elem_bytes == 2 ? kStageH16 : kStageH; }
 constexpr int kSpecialChunk = kConsumerWarps * 32;  // special nodes per work item (one per consumer thread)
 // guard elements before and after the population planes: staged row copies
 // reach one 16-byte chunk beyond a row segment on each side

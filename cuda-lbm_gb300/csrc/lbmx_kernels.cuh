@@ -220,7 +220,7 @@ struct Staging {
     static constexpr int TW = TW_, TH = TH_;
     static constexpr int ROWS = 2 * kConsumerWarps * 32 / TW;  // tile rows one pass of the consumers covers
     static constexpr int TWP = TW + 2 * A;           // box width: the tile plus one chunk each side
-    static constexpr int NST = sizeof(T) == 4 ? 3 : 4;
+    static constexpr int NST = sizeof(T) == 4 ? 3 : (TW_ * TH_ > kStageW * kStageH ? LBMX_NST16 : 4);
     // one population's box, its slot padded to 128 bytes: every box lands on
     // a 128-byte boundary of shared memory
     static constexpr int BOX_ELEMS = TH * TWP;
@@ -373,6 +373,7 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
 
 template <typename T, int OP, int P, bool LEAN>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
+    constexpr int TW = step_tile_w((int)sizeof(T)), TH = step_tile_h((int)sizeof(T));
     // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
     // work item from a global counter; for an interior tile it bulk-copies
     // the tile into the ring), warps 0-7 consume.  Items 0..special_chunks-1
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     // the interior tiles follow.  full[s] completes when a stage's bytes have
     // landed (or at once for a special chunk); empty[s] when all eight
     // consumer warps are done with it.
-    using St = Staging<T>;
+    using St = Staging<T, TW, TH>;
     double v[6] = {0, 0, 0, 0, 0, 0};
     const int tid = threadIdx.x;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -444,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                 mbar_expect_tx(&full[s], St::STAGE_BYTES);
             }
             __syncwarp();
-            stage_issue<T, P>(a, &tmap, x0, y0, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
+            stage_issue<T, P, TW, TH>(a, &tmap, x0, y0, bufs + (size_t)s * St::STAGE_ELEMS, &full[s]);
         }
         // On the normal path the consumers have waited for every fill.  If
         // they stopped releasing stages, let the fills still unconsumed
@@ -454,7 +455,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                 mbar_wait(&full[j % St::NST], (unsigned)((j / St::NST) & 1), kWaitLimit);
     } else {
         // consumers
-        const int lx = tid % (St::TW / 2), r = tid / (St::TW / 2);
+        const int lx = tid % (St::TW / 2), r0 = tid / (St::TW / 2);
         for (int i = 0;; i++) {
             const int s = i % St::NST;
             if (!mbar_wait(&full[s], (unsigned)((i / St::NST) & 1), kWaitLimit)) {
@@ -466,15 +467,19 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             if (sl.x < 0) {
                 special_chunk<T, OP>(a, -2 - sl.x, tid, v);
             } else {
-                const int x0 = sl.y + 2 * lx, y = sl.z + r;
-                bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
-                if (live && a.special_bits) {
-                    const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
-                    live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
+                const int x0 = sl.y + 2 * lx;
+#pragma unroll 1
+                for (int r = r0; r < TH; r += St::ROWS) {
+                    const int y = sl.z + r;
+                    bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
+                    if (live && a.special_bits) {
+                        const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
+                        live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
+                    }
+                    if (live)
+                        interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y,
+                                                              v);
                 }
-                if (live)
-                    interior_unit<T, OP, P, kStageW, kStageH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0,
-                                                                     y, v);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);
@@ -684,12 +689,14 @@ static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tma
     int dev = 0;
     cudaGetDevice(&dev);
     if (!(configured >> (dev & 63) & 1ull)) {
-        cudaError_t e = cudaFuncSetAttribute(step_kernel<T, OP, P, LEAN>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Staging<T>::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(
+            step_kernel<T, OP, P, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (int)Staging<T, step_tile_w((int)sizeof(T)), step_tile_h((int)sizeof(T))>::SMEM);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    step_kernel<T, OP, P, LEAN><<<grid, kThreads, Staging<T>::SMEM, s>>>(a, tmap);
+    step_kernel<T, OP, P, LEAN>
+        <<<grid, kThreads, Staging<T, step_tile_w((int)sizeof(T)), step_tile_h((int)sizeof(T))>::SMEM, s>>>(a, tmap);
     return cudaGetLastError();
 }
 

@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "liblbmx.so")
+LIB_PATH = os.environ.get("LBMX_LIBRARY") or os.path.join(HERE, "liblbmx.so")
 
 # operators, storage, flags and quirks: the values of include/lbmx.h
 BGK, MRT, CM, CM_OPT = 0, 1, 2, 3
