@@ -10,9 +10,11 @@ half-way moving wall, half-way bounce-back on the other walls, Re = 1000
             then a 256 MB read of a second buffer) -- the 1024^2 lattice,
             38 MB per population set, would otherwise stay in the 129 MB L2.
   e2e       the same metric through the C-ABI with host buffers: fields
-            uploaded from pinned host memory, lbmx_step once per LBM step
-            with the FP64 mass/momentum sums read back every step (the
-            reference copies its moment averages back every step,
+            uploaded from pinned host memory, 1000 LBM steps by one
+            lbmx_step_sums call that reduces the FP64 mass/momentum sums in
+            every step's kernel and copies each step's sums to pinned host
+            memory without stalling the GPU (the reference copies its moment
+            averages back with a blocking copy every step,
             macroscopics.cuh:177), final density and velocity read back.
   variants  FP16 / BF16 offset storage on the same workload, each with the
             relative L2 velocity error against the FP64 oracle after 200
@@ -487,23 +489,28 @@ def main():
         out_u = torch.empty((2, n, n), dtype=torch.float32).pin_memory()
         Le = lbmx.Lattice(n, n, op=c["op"], omega=c["omega"], S=c["S"], wall_u=c["wall_u"], device=local,
                           stream=stream.cuda_stream)
-        import ctypes
-        sums = (ctypes.c_double * 3)()
-        K = args.steps
+        # one upload and boundary setup per 1000 steps (the reference's cavity
+        # runs 100k steps per setup)
+        K = max(args.steps, 1000)
+        # the FP64 mass/momentum sums of every step, read back into pinned
+        # host memory without stalling the GPU (the reference reads its
+        # averages back with a blocking copy every step)
+        sums_ring = torch.zeros((K, 3), dtype=torch.float64).pin_memory()
         for rep in range(2):  # first pass warms up
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             Le.set_flags(h_flags)
             Le.init(h_rho, h_u)
-            for _ in range(K):
-                Le.lib.lbmx_step(Le.h, 1)
-                Le._check(Le.lib.lbmx_moments(Le.h, None, None, sums))
-            Le._check(Le.lib.lbmx_moments(Le.h, out_rho.data_ptr(), out_u.data_ptr(), sums))
+            Le._check(Le.lib.lbmx_step_sums(Le.h, K, lbmx.STEP_STORE_MOMENTS, sums_ring.data_ptr()))
+            Le._check(Le.lib.lbmx_moments(Le.h, out_rho.data_ptr(), out_u.data_ptr(), None))
             e2e_t = time.perf_counter() - t0
+        mass = sums_ring[:, 0].numpy()
         line["e2e"] = {"value": round(nodes * K / e2e_t / 1e6, 1), "unit": "MLUPS",
                        "h2d_bytes_per_step": int(round(13 * nodes / K)),
                        "d2h_bytes_per_step": int(round(24 + 12 * nodes / K)),
-                       "lbm_steps": K, "seconds": round(e2e_t, 4)}
+                       "lbm_steps": K, "seconds": round(e2e_t, 4),
+                       "per_step_readback": "FP64 sums {rho, rho ux, rho uy} of every step (lbmx_step_sums)",
+                       "mass_drift": float(abs(mass[-1] - mass[0]) / mass[0])}
         del Le
 
         # ---- FP64 oracle: L2 error reference and CPU baseline

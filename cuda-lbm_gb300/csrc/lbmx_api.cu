@@ -472,8 +472,9 @@ lbmx_status lbmx_init_from_fields(lbmx_handle* h, const float* rho, const float*
     return LBMX_OK;
 }
 
-// One step (index s = t+1); store: write moments and FP64 sums.
-static lbmx_status run_step(lbmx_handle* h, bool store, bool check) {
+// One step (index s = t+1); store: write moments and FP64 sums; sums: the
+// FP64 sums only; series3: where the last block also writes sums 0..2.
+static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, double* series3 = nullptr) {
     const long long s = h->t + 1;
     StepArgs a = base_args(h);
     set_step(h, a, s);
@@ -519,14 +520,15 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check) {
         a.rho_out = h->rho_out;
         a.u_out = h->u_out;
     }
-    if (store || lagged) {
+    if (store || lagged || sums) {
         a.partials = h->partials;
         a.counter = h->counter;
-        a.sums = store ? h->sums : nullptr;
+        a.sums = (store || sums) ? h->sums : nullptr;
         // lagged CM_OPT: the averages of this step feed the next one
         a.avg_out = lagged ? h->avg : nullptr;
     }
     a.check_finite = check ? 1 : 0;
+    a.series3 = series3;
     LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->tmap, h->p.op, st); }));
     h->t = s;
     return LBMX_OK;
@@ -541,7 +543,8 @@ lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags) {
     if (check) LBMX_CUDA(h, cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream));
     for (int i = 0; i < nsteps; i++) {
         const bool last = i == nsteps - 1;
-        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check);
+        lbmx_status st =
+            run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, (flags & LBMX_STEP_SUMS) != 0);
         if (st != LBMX_OK) return st;
     }
     if (check) {
@@ -553,8 +556,52 @@ lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags) {
     return LBMX_OK;
 }
 
+lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, double* series) {
+    if (!h || !series) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step_sums: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_step_sums: call lbmx_init_from_fields first");
+    if (nsteps < 0) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step_sums: nsteps < 0");
+    cudaSetDevice(h->p.device);
+    const bool check = (flags & LBMX_STEP_CHECK_FINITE) != 0;
+    if (check) LBMX_CUDA(h, cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream));
+    // device memory and pinned host memory: the step kernel writes each
+    // step's sums there itself (no copy between the steps); pageable host
+    // memory: a copy per step
+    cudaPointerAttributes attr;
+    bool direct = false;
+    if (cudaPointerGetAttributes(&attr, series) == cudaSuccess)
+        direct = attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged ||
+                 (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr);
+    else
+        cudaGetLastError();
+    double* dev_series = direct ? static_cast<double*>(attr.devicePointer) : nullptr;
+    for (int i = 0; i < nsteps; i++) {
+        const bool last = i == nsteps - 1;
+        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, true,
+                                  direct ? dev_series + 3 * (size_t)i : nullptr);
+        if (st != LBMX_OK) return st;
+        if (!direct)
+            LBMX_CUDA(h, cudaMemcpyAsync(series + 3 * (size_t)i, h->sums, 3 * sizeof(double), cudaMemcpyDefault,
+                                         h->stream));
+    }
+    if (check) {
+        unsigned int w = 0;
+        LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
+        LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (w) return fail(h, LBMX_ERR_NONFINITE, "lbmx_step_sums: non-finite density at step %lld", h->t);
+    }
+    return LBMX_OK;
+}
+
 lbmx_status lbmx_step(lbmx_handle* h, int32_t nsteps) {
     return lbmx_step_ex(h, nsteps, LBMX_STEP_STORE_MOMENTS);
+}
+
+lbmx_status lbmx_moment_sums_async(lbmx_handle* h, double* sums3) {
+    if (!h || !sums3) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_moment_sums_async: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_moment_sums_async: not initialized");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaMemcpyAsync(sums3, h->sums, 3 * sizeof(double), cudaMemcpyDefault, h->stream));
+    return LBMX_OK;
 }
 
 lbmx_status lbmx_moments(lbmx_handle* h, float* rho, float* u, double* sums3) {

@@ -41,6 +41,7 @@ struct StepArgs {
     double* partials;        // [blocks][6] FP64 block sums when non-null
     unsigned int* counter;   // last-block-done counter for the sums
     double* sums;            // [6] final sums
+    double* series3;         // or null: the last block also writes sums 0..2 here (device-accessible)
     float* avg_out;          // averages produced by the last block (lagged CM_OPT / pre-pass)
     unsigned int* error_word;// bit 0: non-finite density seen, bit 1: a staging wait gave up
     int check_finite;        // look for non-finite densities this step

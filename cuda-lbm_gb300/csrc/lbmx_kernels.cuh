@@ -28,8 +28,10 @@ namespace lbmx {
 constexpr int kThreads = kStepThreads;
 
 // Six FP64 sums of a block -> partials[block]; the last block to finish
-// reduces all partials in a fixed order (deterministic, unlike the
-// reference's float atomicAdd in update_avg_mag, macroscopics.cuh:116-118).
+// reduces all partials in a fixed order, in FP64 (the reference adds float
+// atomics, update_avg_mag, macroscopics.cuh:116-118).  Which tiles a
+// persistent CTA's partial covers depends on the dynamic claims, so two runs
+// agree to FP64 rounding, not bit for bit.
 __device__ __forceinline__ void block_sums(const StepArgs& a, double v[6], long long n_nodes) {
     __shared__ double sh[kThreads / 32][6];
     __shared__ bool is_last;
@@ -75,6 +77,8 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, double v[6], long 
             for (int k = 0; k < 6; k++) s[k] += sh[w][k];
         if (a.sums)
             for (int k = 0; k < 6; k++) a.sums[k] = s[k];
+        if (a.series3)
+            for (int k = 0; k < 3; k++) a.series3[k] = s[k];
         if (a.avg_out) {
             a.avg_out[0] = (float)(s[3] / (double)n_nodes);
             a.avg_out[1] = (float)(s[4] / (double)n_nodes);
@@ -133,7 +137,7 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, doubl
     float uy = jy * inv + 0.5f * Fy / rho;
     if (a.gamma) brinkman<float>(a.gamma[off], rho, ux, uy, Fx, Fy);
     float pimag = 0.f;
-    if (OP == LBMX_CM_OPT || a.partials) {
+    if (OP == LBMX_CM_OPT || (a.partials && a.avg_out)) {
         const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
         const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
         const float pxy = f[5] - f[6] + f[7] - f[8];
@@ -145,12 +149,16 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, doubl
         a.u_out[a.g.plane + off] = uy;
     }
     if (a.partials) {
+        // a node's terms in FP32, accumulated in FP64; the averages' terms
+        // only when averages are produced
         v[0] += rho;
-        v[1] += (double)rho * ux;
-        v[2] += (double)rho * uy;
-        v[3] += rho;
-        v[4] += rho * sqrtf(ux * ux + uy * uy);
-        v[5] += pimag;
+        v[1] += rho * ux;
+        v[2] += rho * uy;
+        if (a.avg_out) {
+            v[3] += rho;
+            v[4] += rho * sqrtf(ux * ux + uy * uy);
+            v[5] += pimag;
+        }
     }
     if (a.check_finite && !isfinite(rho)) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {
@@ -314,7 +322,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     V2 uy = fma(0.5f * Fy, inv, jy * inv);
     if (!LEAN && a.gamma) brinkman<V2>(V2{*reinterpret_cast<const float2*>(a.gamma + off)}, rho, ux, uy, Fx, Fy);
     V2 pimag = splat(0.f, rho);
-    if (OP == LBMX_CM_OPT || (!LEAN && a.partials)) {
+    if (OP == LBMX_CM_OPT || (!LEAN && a.partials && a.avg_out)) {
         // offset form: sum c_x^2 w = sum c_y^2 w = 1/3
         const V2 d = OFS ? (f[5] + f[6]) + ((f[7] + f[8]) + splat(1.0f / 3.0f, rho)) : (f[5] + f[6]) + (f[7] + f[8]);
         const V2 pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
@@ -327,12 +335,19 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         *reinterpret_cast<float2*>(a.u_out + plane + off) = uy.v;
     }
     if (!LEAN && a.partials) {
-        v[0] += (double)rho.v.x + (double)rho.v.y;
-        v[1] += (double)rho.v.x * ux.v.x + (double)rho.v.y * ux.v.y;
-        v[2] += (double)rho.v.x * uy.v.x + (double)rho.v.y * uy.v.y;
-        v[3] += (double)rho.v.x + (double)rho.v.y;
-        v[4] += rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x) + rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y);
-        v[5] += (double)pimag.v.x + (double)pimag.v.y;
+        // the pair's terms in FP32, accumulated in FP64 (one FP64 add per
+        // term per unit: GB300's FP64 rate is a small fraction of its FP32
+        // rate); the averages' terms only when averages are produced
+        const V2 jx2 = rho * ux, jy2 = rho * uy;
+        v[0] += rho.v.x + rho.v.y;
+        v[1] += jx2.v.x + jx2.v.y;
+        v[2] += jy2.v.x + jy2.v.y;
+        if (a.avg_out) {
+            v[3] += rho.v.x + rho.v.y;
+            v[4] += rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x) +
+                    rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y);
+            v[5] += pimag.v.x + pimag.v.y;
+        }
     }
     if (!LEAN && a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {

@@ -24,13 +24,13 @@ MOVING_WALL_BB, ZOU_HE_PRESSURE_RIGHT, ZOU_HE_PARABOLIC_LEFT, HALFWAY_BB = 32, 3
 QUIRK_REST_LAG, QUIRK_ZOUHE_LEFT, QUIRK_MRT_FORCE, QUIRK_IBM_2X2, QUIRK_IBM_CLAMP = 1, 2, 4, 8, 16
 QUIRKS_REFERENCE = 0x1F
 OPTION_LAGGED_AVERAGES = 1
-STEP_STORE_MOMENTS, STEP_CHECK_FINITE = 1, 2
+STEP_STORE_MOMENTS, STEP_CHECK_FINITE, STEP_SUMS = 1, 2, 4
 
 STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INVALID_FLAGS",
           5: "NOT_INITIALIZED", 6: "UNSUPPORTED", 7: "NONFINITE", 8: "TOO_LARGE"}
 
 EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
-            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments",
+            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_moment_sums_async", "lbmx_step_sums",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
             "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc", "lbmx_checkpoint_save",
             "lbmx_checkpoint_load", "lbmx_write_vti", "lbmx_batch_create", "lbmx_batch_destroy",
@@ -88,6 +88,10 @@ def load_library(path=LIB_PATH):
     lib.lbmx_step.argtypes = [vp, ctypes.c_int32]
     lib.lbmx_step_ex.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32]
     lib.lbmx_moments.argtypes = [vp, vp, vp, dp]
+    lib.lbmx_moment_sums_async.argtypes = [vp, vp]
+    lib.lbmx_moment_sums_async.restype = ctypes.c_int32
+    lib.lbmx_step_sums.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
+    lib.lbmx_step_sums.restype = ctypes.c_int32
     lib.lbmx_get_populations.argtypes = [vp, vp]
     lib.lbmx_averages.argtypes = [vp, fp]
     lib.lbmx_ibm_set_markers.argtypes = [vp, vp, ctypes.c_int32]

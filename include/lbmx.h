@@ -88,7 +88,8 @@ enum {
 /* lbmx_step_ex flags */
 enum {
     LBMX_STEP_STORE_MOMENTS = 1u << 0, /* last step stores rho, u and the FP64 sums */
-    LBMX_STEP_CHECK_FINITE = 1u << 1   /* last step flags non-finite densities */
+    LBMX_STEP_CHECK_FINITE = 1u << 1,  /* last step flags non-finite densities */
+    LBMX_STEP_SUMS = 1u << 2           /* every step reduces the FP64 sums (no fields stored) */
 };
 
 /* Replaces the compile-time NX/NY/PERIODIC_* macros and the Scenario
@@ -161,6 +162,20 @@ lbmx_status lbmx_set_brinkman(lbmx_handle* h, const float* gamma);
  * reference's d_rho / d_u), and FP64 sums {rho, rho*ux, rho*uy}.  Any output
  * pointer may be NULL. */
 lbmx_status lbmx_moments(lbmx_handle* h, float* rho, float* u, double* sums3);
+
+/* The FP64 sums {rho, rho*ux, rho*uy} of the last stored step, copied into
+ * sums3 (pinned host or device memory) on the handle's stream without
+ * waiting: they are valid once the stream has reached that point
+ * (lbmx_synchronize, or an event).  The reference reads its sums back with a
+ * blocking copy every step (macroscopics.cuh:177); a loop that reads the
+ * sums of every step this way keeps the GPU busy instead. */
+lbmx_status lbmx_moment_sums_async(lbmx_handle* h, double* sums3);
+
+/* nsteps steps (flags as lbmx_step_ex) that also reduce the FP64 sums of
+ * every step into series[3 * k .. 3 * k + 2] for step k (pinned host or
+ * device memory), copied without waiting; the series is complete once the
+ * stream has reached the end (lbmx_synchronize). */
+lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, double* series);
 
 /* Post-collision populations of the last step, out[9*n], population planes
  * in the reference's velocity order.  Slots whose value streamed out of a

@@ -71,3 +71,38 @@ def test_vti_holds_the_stored_moments(tmp_path):
     v = np.frombuffer(rest[16 + nb:16 + nb + nv], np.float32).reshape(24, 40, 3)
     assert np.array_equal(r, rho)
     assert np.array_equal(v[..., 0], u[0]) and np.array_equal(v[..., 1], u[1]) and not v[..., 2].any()
+
+
+def test_per_step_sums_read_without_waiting():
+    # LBMX_STEP_SUMS reduces the FP64 sums in every step's kernel; the async
+    # readback delivers each step's sums once the stream has reached it
+    import ctypes
+    c = C.random_state(C.cavity_moving_wall(80, 60, op=C.MRT), seed=3)
+    a = C.make_lattice(c)
+    b = C.make_lattice(c)
+    ring = (ctypes.c_double * (3 * 6))()
+    for k in range(6):
+        a.step(1, flags=lbmx.STEP_SUMS)
+        a._check(a.lib.lbmx_moment_sums_async(a.h, ctypes.addressof(ring) + 24 * k))
+    a.synchronize()
+    for k in range(6):
+        b.step(1)
+        _, _, s = b.moments()
+        # the persistent CTAs claim tiles dynamically, so the FP64 partial
+        # sums are added in an order that varies from run to run
+        np.testing.assert_allclose(list(ring[3 * k: 3 * k + 3]), list(s), rtol=1e-13, atol=1e-13)
+
+
+def test_step_sums_series():
+    import ctypes
+    c = C.random_state(C.taylor_green(64, 48, op=C.BGK), seed=4)
+    a = C.make_lattice(c)
+    b = C.make_lattice(c)
+    series = (ctypes.c_double * (3 * 5))()
+    a._check(a.lib.lbmx_step_sums(a.h, 5, lbmx.STEP_STORE_MOMENTS, ctypes.addressof(series)))
+    a.synchronize()
+    for k in range(5):
+        b.step(1)
+        _, _, s = b.moments()
+        np.testing.assert_allclose(list(series[3 * k: 3 * k + 3]), list(s), rtol=1e-13, atol=1e-13)
+    np.testing.assert_array_equal(a.moments()[1], b.moments()[1])
