@@ -165,12 +165,10 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     // claim items in chunks of about 1/16 of a CTA's share: few atomics on
     // large lattices, still one item at a time on small ones
     h->tile_chunk = (int)std::max<long long>(1, items / (16LL * h->num_ctas));
-    const long long blocks = h->num_ctas;
-    if (blocks > h->partial_cap) {
-        cudaFree(h->partials);
-        h->partials = nullptr;
-        LBMX_CUDA(h, cudaMalloc((void**)&h->partials, (size_t)blocks * 6 * sizeof(double)));
-        h->partial_cap = blocks;
+    if (!h->partials) {
+        // the six FP64 grid accumulators (zero between launches)
+        LBMX_CUDA(h, cudaMalloc((void**)&h->partials, 8 * sizeof(double)));
+        LBMX_CUDA(h, cudaMemset(h->partials, 0, 8 * sizeof(double)));
     }
     return LBMX_OK;
 }

@@ -27,7 +27,7 @@ struct lbmx_handle {
     float* u_out = nullptr;        // [2][plane]
     float* staging = nullptr;      // dense [3][n] upload / readback staging
     float* pop_out = nullptr;      // dense [9][n] readback staging
-    double* partials = nullptr;    // [blocks][6]
+    double* partials = nullptr;    // [6] FP64 grid accumulators of the step's sums
     unsigned int* counter = nullptr;
     double* sums = nullptr;        // [6]
     float* avg = nullptr;          // [3]
@@ -56,7 +56,7 @@ struct lbmx_handle {
     unsigned long long* tile_counter = nullptr;
     unsigned int* done_counter = nullptr;
     int tile_chunk = 1;
-    alignas(64) CUtensorMap tmap;  // TMA descriptor of the population planes
+    CUtensorMap tmap;  // the type carries the 64-byte alignment TMA needs  // TMA descriptor of the population planes
     long long partial_cap = 0;
     char err[512] = {0};
 };

@@ -27,65 +27,61 @@ namespace lbmx {
 
 constexpr int kThreads = kStepThreads;
 
-// Six FP64 sums of a block -> partials[block]; the last block to finish
-// reduces all partials in a fixed order, in FP64 (the reference adds float
-// atomics, update_avg_mag, macroscopics.cuh:116-118).  Which tiles a
-// persistent CTA's partial covers depends on the dynamic claims, so two runs
-// agree to FP64 rounding, not bit for bit.
-__device__ __forceinline__ void block_sums(const StepArgs& a, double v[6], long long n_nodes) {
-    __shared__ double sh[kThreads / 32][6];
+// The step's grid sums (mass, momentum and the CM_OPT average terms) are
+// accumulated in exact 64-bit fixed point: each node's FP32 term, scaled by
+// 2^30 and rounded, is added as an integer -- per thread, by warp shuffles,
+// then across warps with integer atomics into six accumulators
+// (partials[0..5]).  Integer addition is associative, so the sums are the
+// same bit for bit whichever CTA claims which tile; a term's rounding is at
+// most 2^-31 (5e-10), and the range (|sum| < 2^33) covers any lattice of up
+// to 2^31 nodes at unit density.  The reference adds float atomics
+// (update_avg_mag, macroscopics.cuh:116-118); FP64 arithmetic, a small
+// fraction of FP32's rate on GB300, appears only in the final conversion.
+using Acc = long long;
+constexpr float kFixScale = 1073741824.0f;  // 2^30
+__device__ __forceinline__ Acc fix(float t) { return __float2ll_rn(t * kFixScale); }
+
+// Grid reduction of the accumulators; the last CTA to finish publishes the
+// sums (sums, series, averages) and zeroes the accumulators for the next launch.
+__device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], long long n_nodes) {
     __shared__ bool is_last;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5;
+    const int lane = tid & 31;
+    const int nsum = a.avg_out ? 6 : 3;
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(a.partials);
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        double t = v[k];
+        if (k >= nsum) break;
+        Acc t = v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) sh[warp][k] = t;
+        if (lane == 0 && t != 0) atomicAdd(acc + k, (unsigned long long)t);
     }
     __syncthreads();
-    const unsigned nblocks = gridDim.x;
-    const unsigned bid = blockIdx.x;
     if (tid == 0) {
-        double t[6] = {0, 0, 0, 0, 0, 0};
-        for (int w = 0; w < kThreads / 32; w++)
-            for (int k = 0; k < 6; k++) t[k] += sh[w][k];
-        for (int k = 0; k < 6; k++) a.partials[(long long)bid * 6 + k] = t[k];
         __threadfence();
-        unsigned done = atomicAdd(a.counter, 1u);
-        is_last = (done == nblocks - 1);
+        const unsigned done = atomicAdd(a.counter, 1u);
+        is_last = (done == gridDim.x - 1);
     }
     __syncthreads();
-    if (!is_last) return;
+    if (!is_last || tid != 0) return;
     __threadfence();
-    double t[6] = {0, 0, 0, 0, 0, 0};
-    for (unsigned b = tid; b < nblocks; b += kThreads)
-        for (int k = 0; k < 6; k++) t[k] += __ldcg(a.partials + (long long)b * 6 + k);
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_down_sync(0xffffffffu, t[k], o);
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < nsum; k++) {
+        s[k] = (double)(long long)__ldcg(acc + k) * (1.0 / (double)kFixScale);
+        acc[k] = 0ull;
     }
-    __syncthreads();
-    if (lane == 0)
-        for (int k = 0; k < 6; k++) sh[warp][k] = t[k];
-    __syncthreads();
-    if (tid == 0) {
-        double s[6] = {0, 0, 0, 0, 0, 0};
-        for (int w = 0; w < kThreads / 32; w++)
-            for (int k = 0; k < 6; k++) s[k] += sh[w][k];
-        if (a.sums)
-            for (int k = 0; k < 6; k++) a.sums[k] = s[k];
-        if (a.series3)
-            for (int k = 0; k < 3; k++) a.series3[k] = s[k];
-        if (a.avg_out) {
-            a.avg_out[0] = (float)(s[3] / (double)n_nodes);
-            a.avg_out[1] = (float)(s[4] / (double)n_nodes);
-            a.avg_out[2] = (float)(s[5] / (double)n_nodes);
-        }
-        *a.counter = 0u;
+    if (a.sums)
+        for (int k = 0; k < 6; k++) a.sums[k] = s[k];
+    if (a.series3)
+        for (int k = 0; k < 3; k++) a.series3[k] = s[k];
+    if (a.avg_out) {
+        a.avg_out[0] = (float)(s[3] / (double)n_nodes);
+        a.avg_out[1] = (float)(s[4] / (double)n_nodes);
+        a.avg_out[2] = (float)(s[5] / (double)n_nodes);
     }
+    *a.counter = 0u;
+    __threadfence();
 }
 
 // Post-stream, post-boundary populations of (x, y); returns the node's flag.
@@ -116,7 +112,7 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
 // code for boundary nodes, so a lattice gets bit-identical results from both
 // (inlined, the two callers may contract multiply-adds differently).
 template <typename T, int OP>
-__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, double v[6]) {
+__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[6]) {
     const long long off = (long long)y * a.g.pitch + x;
     float f[9];
     unsigned outmask;
@@ -149,15 +145,15 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, doubl
         a.u_out[a.g.plane + off] = uy;
     }
     if (a.partials) {
-        // a node's terms in FP32, accumulated in FP64; the averages' terms
-        // only when averages are produced
-        v[0] += rho;
-        v[1] += rho * ux;
-        v[2] += rho * uy;
+        // a node's terms in fixed point; the averages' terms only when
+        // averages are produced
+        v[0] += fix(rho);
+        v[1] += fix(rho * ux);
+        v[2] += fix(rho * uy);
         if (a.avg_out) {
-            v[3] += rho;
-            v[4] += rho * sqrtf(ux * ux + uy * uy);
-            v[5] += pimag;
+            v[3] += fix(rho);
+            v[4] += fix(rho * sqrtf(ux * ux + uy * uy));
+            v[5] += fix(pimag);
         }
     }
     if (a.check_finite && !isfinite(rho)) atomicOr(a.error_word, 1u);
@@ -289,13 +285,12 @@ __device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap
 // finite check (chosen at launch), so the unit is straight-line code.
 template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, bool LEAN = false>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
-                                              double v[6]) {
+                                              Acc v[6]) {
     using St = Staging<T, TW, TH>;
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
     const long long off = (long long)y * g.pitch + x0;
     const long long plane = g.plane;
-    const int pitch = g.pitch;
     // 16-bit storage: f holds the stored offsets f - w throughout (the
     // collision works in offset form); FP32: f itself
     constexpr bool OFS = kOffset<T>;
@@ -335,18 +330,17 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         *reinterpret_cast<float2*>(a.u_out + plane + off) = uy.v;
     }
     if (!LEAN && a.partials) {
-        // the pair's terms in FP32, accumulated in FP64 (one FP64 add per
-        // term per unit: GB300's FP64 rate is a small fraction of its FP32
-        // rate); the averages' terms only when averages are produced
+        // both nodes' terms in fixed point; the averages' terms only when
+        // averages are produced
         const V2 jx2 = rho * ux, jy2 = rho * uy;
-        v[0] += rho.v.x + rho.v.y;
-        v[1] += jx2.v.x + jx2.v.y;
-        v[2] += jy2.v.x + jy2.v.y;
+        v[0] += fix(rho.v.x) + fix(rho.v.y);
+        v[1] += fix(jx2.v.x) + fix(jx2.v.y);
+        v[2] += fix(jy2.v.x) + fix(jy2.v.y);
         if (a.avg_out) {
-            v[3] += rho.v.x + rho.v.y;
-            v[4] += rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x) +
-                    rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y);
-            v[5] += pimag.v.x + pimag.v.y;
+            v[3] += fix(rho.v.x) + fix(rho.v.y);
+            v[4] += fix(rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x)) +
+                    fix(rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y));
+            v[5] += fix(pimag.v.x) + fix(pimag.v.y);
         }
     }
     if (!LEAN && a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
@@ -378,7 +372,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
 // One chunk of special nodes: consumer thread t takes node `first + t` of
 // the special-unit list (two nodes per unit).
 template <typename T, int OP>
-__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, double v[6]) {
+__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, Acc v[6]) {
     const int k = chunk * kSpecialChunk + tid;
     if (k >= 2 * a.nspecial) return;
     const int off = a.special_units[k >> 1];
@@ -398,7 +392,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     // landed (or at once for a special chunk); empty[s] when all eight
     // consumer warps are done with it.
     using St = Staging<T, TW, TH>;
-    double v[6] = {0, 0, 0, 0, 0, 0};
+    Acc v[6] = {0, 0, 0, 0, 0, 0};
     const int tid = threadIdx.x;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* bufs = reinterpret_cast<T*>(smem_raw);
@@ -516,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
 // collision (update_avg_mag, macroscopics.cuh:50-120), for CM_OPT.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a) {
-    double v[6] = {0, 0, 0, 0, 0, 0};
+    Acc v[6] = {0, 0, 0, 0, 0, 0};
     const long long n = (long long)a.g.nx * a.g.ny;
     for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
         const int y = (int)(i / a.g.nx), xx = (int)(i - (long long)y * a.g.nx);
@@ -541,9 +535,9 @@ __global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a)
             const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
             const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
             const float pxy = f[5] - f[6] + f[7] - f[8];
-            v[3] += rho;
-            v[4] += rho * sqrtf(ux * ux + uy * uy);
-            v[5] += sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy);
+            v[3] += fix(rho);
+            v[4] += fix(rho * sqrtf(ux * ux + uy * uy));
+            v[5] += fix(sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy));
         }
     }
     block_sums(a, v, (long long)a.g.nx * a.g.ny);
