@@ -30,6 +30,9 @@ half-way moving wall, half-way bounce-back on the other walls, Re = 1000
             5000 steps, checkpoint every 250): forward and backward times,
             the gradients of the outlet mass flux, and a bounded check
             against FP64 central differences of the oracle.
+  validation  the Taylor-Green vortex (256^2, 2000 steps) against its
+            analytic decay, and the IBM cylinder channel (2048 x 512, Re 100)
+            with its MLUPS, drag and lift in FP32 and FP16 offset storage.
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on the same
             workload, 200 steps.
 
@@ -263,6 +266,74 @@ def bench_ensemble(args, torch, stream, device, hbm):
     return out
 
 
+def bench_validation(args, torch, stream, device):
+    """The two remaining configurations as validation lines.
+
+    Taylor-Green vortex: 256 x 256, fully periodic, BGK, nu 0.01, u0 0.04,
+    2000 steps, velocity amplitude against exp(-2 nu k^2 t) (the lattice,
+    4.7 MB, stays in L2).  Flow past a cylinder: 2048 x 512, Zou-He
+    parabolic inlet (peak 0.05), Zou-He pressure outlet, bounce-back walls,
+    cylinder D = 64 at (256, 256) as 256 IBM markers (multi-direct forcing,
+    4-point Peskin kernel), Re 100 on D and the peak inlet velocity, FP32 and
+    FP16 offset storage: MLUPS with the IBM kernels in the step, and drag and
+    lift after `args.cyl_steps` steps (the start of the run, not the
+    shedding state)."""
+    import cases as C
+    import lbmx
+
+    def lattice(c, storage=0):
+        L = lbmx.Lattice(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], periodic=c["periodic"],
+                         storage=storage, u_bc=c["u_bc"], device=device, stream=stream.cuda_stream)
+        L.set_flags(c["flags"])
+        L.init(np.asarray(c["rho"], np.float32), np.asarray(c["u"], np.float32))
+        if c["markers"] is not None:
+            L.set_markers(c["markers"])
+        return L
+
+    def timed(L, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.step(steps)
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1)
+
+    out = {}
+    n, nu, u0, T = 256, 0.01, 0.04, 2000
+    c = C.taylor_green(n, n, op=C.BGK, nu=nu, u0=u0)
+    L = lattice(c)
+    ms = timed(L, T)
+    _, u, _ = L.moments()
+    u_init = np.asarray(c["u"], np.float64)
+    amp = float((u * u_init).sum() / (u_init * u_init).sum())
+    k = 2 * np.pi / n
+    exact = float(np.exp(-2 * nu * k * k * T))
+    out["taylor_green"] = {"workload": "Taylor-Green 256x256 BGK nu 0.01 u0 0.04, %d steps, L2-resident" % T,
+                           "amplitude": amp, "analytic": exact, "rel_err": abs(amp - exact) / exact,
+                           "MLUPS": round(n * n * T / (ms * 1e-3) / 1e6, 1)}
+    del L
+    nx, ny, D, U = 2048, 512, 64, 0.05
+    markers = C.cylinder_markers(256, 256, D / 2, 256)
+    cyl = {}
+    for storage in (0, 1):
+        c = C.channel(nx, ny, op=C.BGK, nu=U * D / 100.0, u_in=U, inlet="parabolic", outlet="zouhe_p",
+                      markers=markers)
+        L = lattice(c, storage)
+        L.step(10)
+        ms = timed(L, args.cyl_steps)
+        _, dl = L.marker_forces()
+        q = 0.5 * 1.0 * U * U * D
+        cyl[STORAGE_NAME[storage]] = {"MLUPS": round(nx * ny * args.cyl_steps / (ms * 1e-3) / 1e6, 1),
+                                      "drag": float(dl[0]), "lift": float(dl[1]),
+                                      "C_D": float(dl[0]) / q, "C_L": float(dl[1]) / q}
+        del L
+    cyl["f16_drag_rel_diff"] = abs(cyl["f16_offset"]["drag"] - cyl["f32"]["drag"]) / abs(cyl["f32"]["drag"])
+    cyl["workload"] = ("cylinder 2048x512, D 64 at (256,256), 256 IBM markers, BGK, Re 100, Zou-He parabolic inlet "
+                       "0.05, Zou-He pressure outlet, %d steps after 10" % args.cyl_steps)
+    out["cylinder"] = cyl
+    return out
+
+
 def bench_adjoint(args, torch, stream, device):
     """Adjoint of the outlet mass flux (time average over the run) of the
     body-force Brinkman channel: 4096 x 1024, periodic x, half-way bounce-back
@@ -402,6 +473,7 @@ def main():
     ap.add_argument("--ens-steps", type=int, default=64)
     ap.add_argument("--ens-err-count", type=int, default=6)
     ap.add_argument("--ens-err-steps", type=int, default=1000)
+    ap.add_argument("--cyl-steps", type=int, default=2000)
     ap.add_argument("--adj-nx", type=int, default=4096)
     ap.add_argument("--adj-ny", type=int, default=1024)
     ap.add_argument("--adj-steps", type=int, default=5000)
@@ -558,6 +630,8 @@ def main():
         line["ensemble"] = bench_ensemble(args, torch, stream, local, hbm)
         # ---- adjoint of the Brinkman channel
         line["adjoint"] = bench_adjoint(args, torch, stream, local)
+        # ---- Taylor-Green decay and the IBM cylinder
+        line["validation"] = bench_validation(args, torch, stream, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
