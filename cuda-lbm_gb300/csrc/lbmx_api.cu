@@ -41,9 +41,9 @@ static lbmx_status fail(lbmx_handle* h, lbmx_status code, const char* fmt, ...) 
 
 size_t lbmx::elem_size(int storage) { return storage == LBMX_STORAGE_F32 ? 4 : 2; }
 
-// 3-D tiled TMA descriptor over the population planes: dims {pitch, ny,
-// planes}; box {tile_w + 2 chunks of 16 bytes, tile_h, 1}; out-of-range
-// elements read as zero.  cuTensorMapEncodeTiled comes from the driver
+// 3-D tiled TMA descriptor over the population planes: dims {nx, ny,
+// planes}, row stride pitch; box {tile_w + 2 chunks of 16 bytes, tile_h, 1};
+// out-of-range elements read as zero.  cuTensorMapEncodeTiled comes from the driver
 // through the runtime's entry-point query (no link against libcuda).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -64,7 +64,9 @@ bool lbmx::encode_population_map(const lbmx_handle* h, CUtensorMap* out, int til
     const CUtensorMapDataType dt = h->p.storage == LBMX_STORAGE_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                    : h->p.storage == LBMX_STORAGE_F16_OFFSET ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                                              : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-    const cuuint64_t dims[3] = {(cuuint64_t)h->g.pitch, (cuuint64_t)h->g.ny, (cuuint64_t)h->nplanes};
+    // the row extent is nx, not the padded pitch: box columns past the
+    // lattice are zero-filled by the TMA unit without reading memory
+    const cuuint64_t dims[3] = {(cuuint64_t)h->g.nx, (cuuint64_t)h->g.ny, (cuuint64_t)h->nplanes};
     const cuuint64_t strides[2] = {(cuuint64_t)h->g.pitch * es, (cuuint64_t)h->g.plane * es};
     const cuuint32_t box[3] = {(cuuint32_t)(tile_w + 2 * 16 / es), (cuuint32_t)tile_h, 1u};
     const cuuint32_t estr[3] = {1u, 1u, 1u};
