@@ -196,6 +196,58 @@ def run_cpu_oracle(n, steps, threads):
     return u, (n * n * (steps - 1)) / dt / 1e6, dt
 
 
+def bench_steady(args, torch, stream, device):
+    """The cavity run towards steady state in FP32, FP16 and BF16 offset
+    storage: the 16-bit forms' relative L2 velocity error against FP32 after
+    `args.steady_steps` steps (FP32 and FP64 agree to ~1e-6 at 200 steps, so
+    this is the error against FP64 to that accuracy), how far from steady the
+    flow still is (relative change of u over the last 1000 steps), and the
+    sustained MLUPS of the long run (no L2 flush; the 1024^2 FP32 lattice is
+    75 MB).  With --steady-fp64, the same at 256^2 (Re 1000) against the
+    FP64 oracle's own run on the host cores."""
+    import lbmx
+
+    def run(n, storage, steps):
+        c = cavity_case(n)
+        L = lbmx.Lattice(n, n, op=c["op"], omega=c["omega"], S=c["S"], storage=storage, wall_u=c["wall_u"],
+                         device=device, stream=stream.cuda_stream)
+        L.set_flags(c["flags"])
+        L.init(np.ones((n, n), np.float32), np.zeros((2, n, n), np.float32))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.step(steps - 1000)
+        e1.record(stream)
+        _, ua, _ = L.moments()
+        L.step(1000)
+        _, ub, _ = L.moments()
+        ms = e0.elapsed_time(e1)
+        return ub, l2_error(ub, ua), n * n * (steps - 1000) / (ms * 1e-3) / 1e6
+
+    out = {"workload": "lid-driven cavity %dx%d MRT, lid 0.1, Re 1000, %d steps from rest"
+                       % (args.size, args.size, args.steady_steps)}
+    u32, res32, m32 = run(args.size, 0, args.steady_steps)
+    out["f32"] = {"residual_last_1000_steps": res32, "MLUPS_sustained": round(m32, 1)}
+    for storage in (1, 2):
+        u, res, m = run(args.size, storage, args.steady_steps)
+        out[STORAGE_NAME[storage]] = {"l2_u_err_vs_f32": l2_error(u, u32), "residual_last_1000_steps": res,
+                                      "MLUPS_sustained": round(m, 1)}
+    if args.steady_fp64:
+        import cases as C
+        n = 256
+        o = C.make_oracle(cavity_case(n))
+        t0 = time.perf_counter()
+        o.step(args.steady_steps)
+        dt = time.perf_counter() - t0
+        _, u64, _ = o.moments()
+        small = {"workload": "lid-driven cavity 256x256 MRT, lid 0.1, Re 1000, %d steps; FP64 oracle on %d host "
+                             "threads (%.0f s)" % (args.steady_steps, os.cpu_count() or 1, dt)}
+        for storage in (0, 1, 2):
+            u, res, _ = run(n, storage, args.steady_steps)
+            small[STORAGE_NAME[storage]] = {"l2_u_err_vs_fp64": l2_error(u, u64), "residual_last_1000_steps": res}
+        out["fp64_256"] = small
+    return out
+
+
 def bench_ensemble(args, torch, stream, device, hbm):
     """Batched ensemble: `args.ens_count` lid-driven cavities (sides uniform in
     {64, ..., 768}, Re log-uniform in [100, 5000], seed 0), D2Q9 MRT, advanced
@@ -331,7 +383,94 @@ def bench_validation(args, torch, stream, device):
     cyl["workload"] = ("cylinder 2048x512, D 64 at (256,256), 256 IBM markers, BGK, Re 100, Zou-He parabolic inlet "
                        "0.05, Zou-He pressure outlet, %d steps after 10" % args.cyl_steps)
     out["cylinder"] = cyl
+    out["drag_sensitivity"] = bench_drag_sensitivity(args, torch, stream, device)
     return out
+
+
+def bench_drag_sensitivity(args, torch, stream, device):
+    """d(mean drag)/d(inlet velocity) of the cylinder configuration by the
+    tangent-linear model (lbmx_tangent_*), over steps T/2+1..T from rest.
+    Checked two ways: against a central difference (h = 1% of the inlet
+    velocity) of the engine's own FP32 drag series at full size, and on a
+    112 x 44 channel (cylinder D 12, 36 markers, 400 steps) against central
+    differences of the FP64 oracle."""
+    import cases as C
+    import lbmx
+
+    nx, ny, D, U, T = 2048, 512, 64, 0.05, args.cyl_steps
+    half = T // 2
+    mk = C.cylinder_markers(256, 256, D / 2, 256)
+
+    def case(u):
+        return C.channel(nx, ny, op=C.BGK, nu=U * D / 100.0, u_in=u, inlet="parabolic", outlet="zouhe_p", markers=mk)
+
+    c = case(U)
+    t = lbmx.Tangent(nx, ny, lbmx.TANGENT_U_BC, op=c["op"], omega=c["omega"], S=c["S"], flags=c["flags"], u_bc=U,
+                     device=device, stream=stream.cuda_stream)
+    t.set_state(np.ones((ny, nx), np.float32), np.zeros((2, ny, nx), np.float32))
+    t.set_markers(mk)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s = t.run(T)
+    e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1)
+    del t
+    deriv = float(s[half:, 2].mean())
+
+    def engine_mean_drag(u):
+        L = lbmx.Lattice(nx, ny, op=c["op"], omega=c["omega"], S=c["S"], u_bc=u, device=device,
+                         stream=stream.cuda_stream)
+        L.set_flags(c["flags"])
+        L.init(np.ones((ny, nx), np.float32), np.zeros((2, ny, nx), np.float32))
+        L.set_markers(mk)
+        L.step(half)
+        d = []
+        for _ in range(T - half):
+            L.step(1)
+            d.append(L.marker_forces()[1][0])
+        return float(np.mean(d))
+
+    h = 0.01 * U
+    fd = (engine_mean_drag(U + h) - engine_mean_drag(U - h)) / (2 * h)
+
+    # bounded FP64 check
+    import oracle as O
+    mk_s = C.cylinder_markers(30.3, 21.7, 6.0, 36)
+    cs = C.channel(112, 44, op=C.BGK, nu=0.04, u_in=0.05, inlet="parabolic", outlet="zouhe_p", markers=mk_s)
+    ts = lbmx.Tangent(112, 44, lbmx.TANGENT_U_BC, op=cs["op"], omega=cs["omega"], S=cs["S"], flags=cs["flags"],
+                      u_bc=0.05, device=device, stream=stream.cuda_stream)
+    ts.set_state(np.ones((44, 112), np.float32), np.zeros((2, 44, 112), np.float32))
+    ts.set_markers(mk_s)
+    ss = ts.run(400)
+    del ts
+
+    def oracle_mean_drag(u):
+        o = O.Oracle(112, 44, op=cs["op"], omega=cs["omega"], S=cs["S"], u_bc=u, precision="f64")
+        o.set_flags(cs["flags"])
+        o.init(cs["rho"], cs["u"])
+        o.set_markers(mk_s)
+        d = []
+        for k in range(400):
+            o.step(1)
+            if k >= 200:
+                d.append(-o.markers()[2][0].sum())
+        return float(np.mean(d))
+
+    hs = 1e-4
+    fd64 = (oracle_mean_drag(0.05 + hs) - oracle_mean_drag(0.05 - hs)) / (2 * hs)
+    d_small = float(ss[200:, 2].mean())
+    return {"workload": "cylinder 2048x512 as above, BGK, %d steps from rest; J = mean drag over steps %d..%d"
+                        % (T, half + 1, T),
+            "parameter": "inlet peak velocity u_in = 0.05",
+            "method": "tangent-linear (forward mode) through the engine's per-node code and IBM rounds",
+            "mean_drag": float(s[half:, 0].mean()), "d_mean_drag_d_u_in": deriv,
+            "d_mean_lift_d_u_in": float(s[half:, 3].mean()),
+            "engine_fp32_central_fd_h_1pct": fd, "rel_diff_vs_engine_fd": abs(deriv - fd) / abs(fd),
+            "tangent_ms": round(ms, 2), "tangent_MLUPS": round(nx * ny * T / (ms * 1e-3) / 1e6, 1),
+            "fp64_check": {"workload": "channel 112x44, cylinder D 12 at (30.3, 21.7), 36 markers, 400 steps, "
+                                       "J = mean drag over steps 201..400, FP64 oracle central difference h = 1e-4",
+                           "tangent": d_small, "fp64_fd": fd64, "rel_err": abs(d_small - fd64) / abs(fd64)}}
 
 
 def bench_adjoint(args, torch, stream, device):
@@ -474,6 +613,9 @@ def main():
     ap.add_argument("--ens-err-count", type=int, default=6)
     ap.add_argument("--ens-err-steps", type=int, default=1000)
     ap.add_argument("--cyl-steps", type=int, default=2000)
+    ap.add_argument("--steady-steps", type=int, default=100000)
+    ap.add_argument("--steady-fp64", action="store_true",
+                    help="also run the 256^2 cavity to steady state against the FP64 oracle (about a minute of CPU)")
     ap.add_argument("--adj-nx", type=int, default=4096)
     ap.add_argument("--adj-ny", type=int, default=1024)
     ap.add_argument("--adj-steps", type=int, default=5000)
@@ -608,6 +750,8 @@ def main():
             del Lv, Lw
         variants["f16_speedup_vs_f32"] = round(variants["f16_offset"]["MLUPS"] / variants["f32"]["MLUPS"], 3)
         line["variants"] = variants
+        # ---- the same cavity run towards steady state
+        line["steady_state"] = bench_steady(args, torch, stream, local)
 
         # ---- HBM-bound size, no flush needed
         hn = args.hbm_size

@@ -16,7 +16,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbmx.so")
 
 SOURCES = ["lbmx_api.cu", "lbmx_ibm.cu", "lbmx_step_f32.cu", "lbmx_step_f16.cu", "lbmx_step_bf16.cu",
-           "lbmx_noalloc.cu", "lbmx_batch.cu", "lbmx_batch_f32.cu", "lbmx_batch_f16.cu", "lbmx_batch_bf16.cu", "lbmx_adjoint.cu"]
+           "lbmx_noalloc.cu", "lbmx_batch.cu", "lbmx_batch_f32.cu", "lbmx_batch_f16.cu", "lbmx_batch_bf16.cu", "lbmx_adjoint.cu",
+           "lbmx_tangent.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + os.path.join(REPO, "include"), "-I" + CSRC]

@@ -109,6 +109,7 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.tile_counter = h->tile_counter;
     a.done_counter = h->done_counter;
     a.tile_chunk = h->tile_chunk;
+    a.sr = (h->p.storage != LBMX_STORAGE_F32 && !(h->p.options & LBMX_OPTION_ROUND_NEAREST)) ? 1 : 0;
     return a;
 }
 
@@ -192,6 +193,7 @@ static lbmx_status check_pipeline(lbmx_handle* h) {
 void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.parity = (int)(s & 1);
     a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? (a.parity ? 9 : 0) : 0;
+    a.sr_seed = sr_seed_of(s);
     // interior store targets: parity 1 -> slot q of the node x + c_q,
     // parity 0 -> the node's own slot OPP(q) (D2Q9 order: rest, E, N, W, S, NE, NW, SW, SE)
     static const int cx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
@@ -656,6 +658,8 @@ lbmx_status lbmx_averages(lbmx_handle* h, float* avg3) {
     return LBMX_OK;
 }
 
+}  // extern "C"
+
 // Peskin 4-point kernel (src/IBM/IBMUtils.cuh:24-33), evaluated in double on the host
 static double delta4(double r) {
     const double a = std::fabs(r);
@@ -664,33 +668,24 @@ static double delta4(double r) {
     return 0.0;
 }
 
-lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
-    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: NULL handle");
-    if (n < 0 || (n > 0 && !xy)) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: bad marker array");
-    cudaSetDevice(h->p.device);
-    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
-    free_ibm(h);
-    if (n == 0) return rebuild_special(h);
-    const Geometry& g = h->g;
-    std::vector<float> hxy(2 * (size_t)n);
-    LBMX_CUDA(h, cudaMemcpy(hxy.data(), xy, 2 * (size_t)n * sizeof(float), cudaMemcpyDefault));
-    const bool two = (h->p.quirks & LBMX_QUIRK_IBM_2X2) != 0;
+namespace lbmx {
+int ibm_build_stencil(int nx, int ny, long long pitch, bool two, const float* hxy, int n, std::vector<int>& sidx,
+                      std::vector<float>& sw, std::vector<int>& nodes) {
     const int S = two ? 2 : 4, lo = two ? 0 : -1, S2 = S * S;
-    std::vector<int> sidx((size_t)n * S2, -1);
-    std::vector<float> sw((size_t)n * S2, 0.f);
-    std::vector<int> nodes;
+    sidx.assign((size_t)n * S2, -1);
+    sw.assign((size_t)n * S2, 0.f);
+    nodes.clear();
     std::unordered_map<long long, int> map;
     for (int k = 0; k < n; k++) {
         const float px = hxy[2 * k], py = hxy[2 * k + 1];
-        if (!std::isfinite(px) || !std::isfinite(py))
-            return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: marker %d is not finite", k);
+        if (!std::isfinite(px) || !std::isfinite(py)) return k;
         const float gx = std::floor(px), gy = std::floor(py);
         // x offset outer, y offset inner, as the reference's stencil loops (IBM_impl.cu:19-20)
         for (int i = 0; i < S; i++)
             for (int j = 0; j < S; j++) {
                 const int xn = (int)(gx + (float)(lo + i)), yn = (int)(gy + (float)(lo + j));
-                if (xn < 0 || xn >= g.nx || yn < 0 || yn >= g.ny) continue;
-                const long long off = (long long)yn * g.pitch + xn;
+                if (xn < 0 || xn >= nx || yn < 0 || yn >= ny) continue;
+                const long long off = (long long)yn * pitch + xn;
                 auto it = map.find(off);
                 int idx;
                 if (it == map.end()) {
@@ -704,6 +699,28 @@ lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
                 sw[(size_t)k * S2 + i * S + j] = (float)(delta4((double)px - xn) * delta4((double)py - yn));
             }
     }
+    return -1;
+}
+}  // namespace lbmx
+
+extern "C" {
+
+lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: NULL handle");
+    if (n < 0 || (n > 0 && !xy)) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: bad marker array");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    free_ibm(h);
+    if (n == 0) return rebuild_special(h);
+    const Geometry& g = h->g;
+    std::vector<float> hxy(2 * (size_t)n);
+    LBMX_CUDA(h, cudaMemcpy(hxy.data(), xy, 2 * (size_t)n * sizeof(float), cudaMemcpyDefault));
+    const bool two = (h->p.quirks & LBMX_QUIRK_IBM_2X2) != 0;
+    const int S = two ? 2 : 4, S2 = S * S;
+    std::vector<int> sidx, nodes;
+    std::vector<float> sw;
+    const int bad = lbmx::ibm_build_stencil(g.nx, g.ny, g.pitch, two, hxy.data(), n, sidx, sw, nodes);
+    if (bad >= 0) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: marker %d is not finite", bad);
     const int np = (int)nodes.size();
     if (lbmx::ibm_smem_bytes(np, n) > 200 * 1024)
         return fail(h, LBMX_ERR_TOO_LARGE, "lbmx_ibm_set_markers: %d markers touch %d nodes; limit is 200 KB of patch state",

@@ -35,6 +35,7 @@ struct lbmx_batch {
     unsigned long long* counter = nullptr;
     unsigned int* done = nullptr;
     unsigned int* error_word = nullptr;
+    unsigned int* step = nullptr;      // step index of the next launch (rounding hash seed)
     std::vector<StepArgs> host_args;   // what d_args holds
     int args_tile_w = 0, args_tile_h = 0;  // tile shape d_tmaps / d_items were built for
     bool lean = false;                     // no lattice has a per-node force or Brinkman field
@@ -181,6 +182,7 @@ static lbmx_status launch_one(lbmx_batch* b, long long s, int variant) {
     ba.counter = b->counter;
     ba.done = b->done;
     ba.error_word = b->error_word;
+    ba.step = b->step;
     const unsigned grid = (unsigned)std::max(1, std::min(b->nitems, b->cfg.ctas_per_sm * b->num_sms));
     // plain steps of lattices without per-node force or Brinkman fields run
     // the kernel without those branches
@@ -222,8 +224,15 @@ static lbmx_status build_graphs(lbmx_batch* b) {
     return LBMX_OK;
 }
 
+__global__ void set_step_word(unsigned int* w, unsigned int v) { *w = v; }
+
 // nsteps steps from step count t; last_variant for the final step.
 static lbmx_status run_steps(lbmx_batch* b, long long t, int nsteps, int last_variant) {
+    // the kernels take the step index for the stochastic-rounding hash from
+    // the device (graph replays cannot carry it as an argument); each launch
+    // advances it
+    set_step_word<<<1, 1, 0, b->stream>>>(b->step, (unsigned int)(t + 1));
+    BATCH_CUDA(b, cudaGetLastError());
     int i = 0;
     while (i < nsteps) {
         const int left = nsteps - i;
@@ -287,7 +296,7 @@ void lbmx_batch_destroy(lbmx_batch* b) {
     else cudaDeviceSynchronize();
     drop_graphs(b);
     cudaFree(b->d_args); cudaFree(b->d_tmaps); cudaFree(b->d_items);
-    cudaFree(b->counter); cudaFree(b->done); cudaFree(b->error_word);
+    cudaFree(b->counter); cudaFree(b->done); cudaFree(b->error_word); cudaFree(b->step);
     for (cudaEvent_t e : b->stream_events) cudaEventDestroy(e);
     if (b->end_event) cudaEventDestroy(b->end_event);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -352,8 +361,10 @@ lbmx_status lbmx_batch_create(lbmx_handle* const* lattices, int32_t count, lbmx_
     }
     if (cudaMalloc((void**)&b->counter, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void**)&b->done, sizeof(unsigned int)) != cudaSuccess ||
-        cudaMalloc((void**)&b->error_word, sizeof(unsigned int)) != cudaSuccess)
+        cudaMalloc((void**)&b->error_word, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc((void**)&b->step, sizeof(unsigned int)) != cudaSuccess)
         return cleanup(LBMX_ERR_OUT_OF_MEMORY, "cudaMalloc failed");
+    cudaMemsetAsync(b->step, 0, sizeof(unsigned int), b->stream);
     cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), b->stream);
     cudaMemsetAsync(b->done, 0, sizeof(unsigned int), b->stream);
     cudaMemsetAsync(b->error_word, 0, sizeof(unsigned int), b->stream);

@@ -28,6 +28,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
     uint64_t* empty = full + St::NST;
     int4* slot = reinterpret_cast<int4*>(empty + St::NST);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // every lattice of the batch stands at this step index (the last CTA of
+    // the previous launch advanced it)
+    const uint32_t seed = sr_seed_of((long long)*b.step);
     if (tid == 0) {
         for (int s = 0; s < St::NST; s++) {
             mbar_init(&full[s], 1);
@@ -108,10 +111,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
                     }
                     if (live)
-                        interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v);
+                        interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v,
+                                                              seed);
                 }
             } else {
-                special_chunk<T, OP>(a, -2 - sl.x, tid, v);
+                special_chunk<T, OP>(a, -2 - sl.x, tid, v, seed);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);
@@ -123,6 +127,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
         if (atomicAdd(b.done, 1u) == gridDim.x - 1) {
             *b.counter = 0ull;
             *b.done = 0u;
+            *b.step += 1u;
             __threadfence();
         }
     }

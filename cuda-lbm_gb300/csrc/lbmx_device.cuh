@@ -62,14 +62,68 @@ __device__ __forceinline__ float vpos_or(float a, float alt) { return a > 0.f ? 
 // ---------------------------------------------------------------- storage
 // FP32 stores f itself; the 16-bit forms store the offset f - w_q, which is
 // O(|u|) instead of O(1) and so keeps 10 (FP16) or 7 (BF16) significant bits
-// for the part of f that carries the flow.
+// for the part of f that carries the flow.  FP16 holds the offset times
+// 2^12 (exact both ways), so offsets down to 2^-26 stay in FP16's normal
+// range instead of its coarse subnormals.
+//
+// Stores round stochastically by default: up with probability equal to the
+// discarded fraction of the gap to the next representable value (Forsythe
+// 1959; Connolly, Higham & Mary 2021), so each store is unbiased,
+// E[stored] = exact.  Rounding to nearest gives a steady flow the same
+// rounding error at every node every step -- a persistent source term whose
+// effect the slow viscous modes amplify with the lattice size (about 1/(nu k^2)
+// steps of it); stochastic errors are independent from step to step and
+// average out instead.  The random bits come from a counter-based hash of
+// (node offset, step), so a run is still bitwise reproducible.
 template <typename T> struct Store;
 //
 // ld/st/ld2/st2 convert between f and the stored form; ldr/str/ld2r/st2r move
 // the stored value itself (f for FP32, f - w for the 16-bit forms), for code
-// that computes with offsets directly (kOffset<T>).
+// that computes with offsets directly (kOffset<T>); the *_sr forms take
+// random bits (sr_bits) and round stochastically.
 template <typename T>
 constexpr bool kOffset = sizeof(T) == 2;
+
+// 32 well-mixed bits of a unit (two x-neighbouring nodes, even offset) and
+// the step seed: the "lowbias32" integer finaliser (C. Wellons,
+// hash-prospector) of a Weyl-scrambled key.  The odd node of the unit
+// multiplies it by an odd constant.
+__device__ __forceinline__ uint32_t sr_hash(uint32_t unit, uint32_t seed) {
+    uint32_t h = unit * 0x9E3779B1u ^ seed;
+    h ^= h >> 16;
+    h *= 0x7FEB352Du;
+    h ^= h >> 15;
+    h *= 0x846CA68Bu;
+    h ^= h >> 16;
+    return h;
+}
+__device__ __forceinline__ uint32_t sr_odd(uint32_t h) { return h * 0xA24BAED5u; }
+__device__ __forceinline__ uint32_t sr_node_hash(uint32_t off, uint32_t seed) {
+    const uint32_t h = sr_hash(off >> 1, seed);
+    return (off & 1u) ? sr_odd(h) : h;
+}
+// random bits of population q from a node's hash: an odd multiplier per q
+// (a bijection of the 32-bit hash, whose top bits are then uniform)
+__device__ __forceinline__ uint32_t sr_bits(uint32_t h, int q) { return h * (0x2545F491u + 0x9E3779B8u * (uint32_t)q); }
+
+// Stochastic FP32 -> FP16 in two exact steps: 13 random bits added below
+// FP16's last mantissa bit, the 13 bits cleared, then a round-to-nearest
+// conversion that finds the value already representable (in FP16's normal
+// range) -- so overflow still gives Inf and NaN stays NaN, and two values
+// convert in one packed instruction.
+__device__ __forceinline__ float sr_cut16(float x, uint32_t r) {
+    return __uint_as_float((__float_as_uint(x) + (r >> 19)) & 0xFFFFE000u);
+}
+__device__ __forceinline__ __half sr_half(float x, uint32_t r) { return __float2half_rn(sr_cut16(x, r)); }
+// FP32 -> BF16: 16 random bits added below BF16's last mantissa bit, then
+// the high half of the word is the result (Inf + bits is NaN, NaN stays NaN)
+__device__ __forceinline__ uint32_t sr_bf16_bits(float x, uint32_t r) { return __float_as_uint(x) + (r >> 16); }
+__device__ __forceinline__ __nv_bfloat16 sr_bf16(float x, uint32_t r) {
+    __nv_bfloat16_raw b;
+    b.x = (unsigned short)(sr_bf16_bits(x, r) >> 16);
+    return __nv_bfloat16(b);
+}
+
 template <> struct Store<float> {
     static __device__ __forceinline__ float ldr(const float* p) { return *p; }
     static __device__ __forceinline__ float2 ld2r(const float* p) { return *reinterpret_cast<const float2*>(p); }
@@ -79,25 +133,35 @@ template <> struct Store<float> {
     static __device__ __forceinline__ void st(float* p, float v, float) { *p = v; }
     static __device__ __forceinline__ float2 ld2(const float* p, float) { return *reinterpret_cast<const float2*>(p); }
     static __device__ __forceinline__ void st2(float* p, float2 v, float) { *reinterpret_cast<float2*>(p) = v; }
+    static __device__ __forceinline__ void str_sr(float* p, float v, uint32_t) { *p = v; }
+    static __device__ __forceinline__ void st2r_sr(float* p, float2 v, uint32_t, uint32_t) {
+        *reinterpret_cast<float2*>(p) = v;
+    }
+    static __device__ __forceinline__ void st_sr(float* p, float v, float, uint32_t) { *p = v; }
 };
 template <> struct Store<__half> {
-    static __device__ __forceinline__ float ldr(const __half* p) { return __half2float(*p); }
+    static constexpr float kUp = 4096.0f, kDown = 1.0f / 4096.0f;  // 2^12 storage scale
+    static __device__ __forceinline__ float ldr(const __half* p) { return __half2float(*p) * kDown; }
     static __device__ __forceinline__ float2 ld2r(const __half* p) {
-        return __half22float2(*reinterpret_cast<const __half2*>(p));
+        return __fmul2_rn(__half22float2(*reinterpret_cast<const __half2*>(p)), make_float2(kDown, kDown));
     }
-    static __device__ __forceinline__ void str(__half* p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ void str(__half* p, float v) { *p = __float2half_rn(v * kUp); }
     static __device__ __forceinline__ void st2r(__half* p, float2 v) {
-        *reinterpret_cast<__half2*>(p) = __float22half2_rn(v);
+        *reinterpret_cast<__half2*>(p) = __float22half2_rn(__fmul2_rn(v, make_float2(kUp, kUp)));
     }
-    static __device__ __forceinline__ float ld(const __half* p, float w) { return w + __half2float(*p); }
-    static __device__ __forceinline__ void st(__half* p, float v, float w) { *p = __float2half_rn(v - w); }
+    static __device__ __forceinline__ float ld(const __half* p, float w) { return w + ldr(p); }
+    static __device__ __forceinline__ void st(__half* p, float v, float w) { str(p, v - w); }
     static __device__ __forceinline__ float2 ld2(const __half* p, float w) {
-        const float2 d = __half22float2(*reinterpret_cast<const __half2*>(p));
+        const float2 d = ld2r(p);
         return make_float2(d.x + w, d.y + w);
     }
-    static __device__ __forceinline__ void st2(__half* p, float2 v, float w) {
-        *reinterpret_cast<__half2*>(p) = __float22half2_rn(make_float2(v.x - w, v.y - w));
+    static __device__ __forceinline__ void st2(__half* p, float2 v, float w) { st2r(p, make_float2(v.x - w, v.y - w)); }
+    static __device__ __forceinline__ void str_sr(__half* p, float v, uint32_t r) { *p = sr_half(v * kUp, r); }
+    static __device__ __forceinline__ void st2r_sr(__half* p, float2 v, uint32_t r0, uint32_t r1) {
+        const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
+        *reinterpret_cast<__half2*>(p) = __float22half2_rn(make_float2(sr_cut16(s.x, r0), sr_cut16(s.y, r1)));
     }
+    static __device__ __forceinline__ void st_sr(__half* p, float v, float w, uint32_t r) { str_sr(p, v - w, r); }
 };
 template <> struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ float ldr(const __nv_bfloat16* p) { return __bfloat162float(*p); }
@@ -116,6 +180,14 @@ template <> struct Store<__nv_bfloat16> {
     }
     static __device__ __forceinline__ void st2(__nv_bfloat16* p, float2 v, float w) {
         *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn(make_float2(v.x - w, v.y - w));
+    }
+    static __device__ __forceinline__ void str_sr(__nv_bfloat16* p, float v, uint32_t r) { *p = sr_bf16(v, r); }
+    static __device__ __forceinline__ void st2r_sr(__nv_bfloat16* p, float2 v, uint32_t r0, uint32_t r1) {
+        // the two high halves in one word
+        *reinterpret_cast<uint32_t*>(p) = __byte_perm(sr_bf16_bits(v.x, r0), sr_bf16_bits(v.y, r1), 0x7632);
+    }
+    static __device__ __forceinline__ void st_sr(__nv_bfloat16* p, float v, float w, uint32_t r) {
+        str_sr(p, v - w, r);
     }
 };
 
@@ -185,12 +257,19 @@ __device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y
 // node's own free slot OPP(q); parity 0: to slot OPP(q) of x.
 template <typename T>
 __device__ __forceinline__ void store_post_collision(const StepArgs& a, int x, int y, const float f[9],
-                                                     unsigned outmask, uint8_t fl) {
+                                                     unsigned outmask, uint8_t fl, uint32_t seed) {
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
     const long long row = (long long)y * g.pitch;
     const bool hw = is_halfway(fl);
-    Store<T>::st(F + a.rest_plane * g.plane + row + x, f[0], WQ(0));
+    const bool sr = kOffset<T> && a.sr;
+    const uint32_t h = sr ? sr_node_hash((uint32_t)(row + x), seed) : 0u;
+    // the value f of population q goes to p, rounded as configured
+    auto put = [&](T* p, float v, int q) {
+        if (sr) Store<T>::st_sr(p, v, WQ(q), sr_bits(h, q));
+        else Store<T>::st(p, v, WQ(q));
+    };
+    put(F + a.rest_plane * g.plane + row + x, f[0], 0);
 #pragma unroll
     for (int q = 1; q < 9; q++) {
         if (a.parity) {
@@ -204,10 +283,10 @@ __device__ __forceinline__ void store_post_collision(const StepArgs& a, int x, i
                 if (g.periodic_y) dy = dy < 0 ? dy + g.ny : dy - g.ny;
                 else out = true;
             }
-            if (!out) Store<T>::st(F + q * g.plane + (long long)dy * g.pitch + dx, f[q], WQ(q));
-            else if (hw) Store<T>::st(F + OPP(q) * g.plane + row + x, f[q] - wall_term(a, q, fl), WQ(q));
+            if (!out) put(F + q * g.plane + (long long)dy * g.pitch + dx, f[q], q);
+            else if (hw) put(F + OPP(q) * g.plane + row + x, f[q] - wall_term(a, q, fl), q);
         } else {
-            Store<T>::st(F + OPP(q) * g.plane + row + x, f[q], WQ(q));
+            put(F + OPP(q) * g.plane + row + x, f[q], q);
         }
     }
     if (outmask && !hw) {
@@ -231,8 +310,13 @@ __device__ __forceinline__ float feq_bc(int q, float rho, float ux, float uy) {
     return WQ(q) * rho * (1.0f + cu / cs2 + cu * cu / (2.0f * cs2 * cs2) - uu / (2.0f * cs2));
 }
 
+// The Zou-He and bounce-back functors are templates over the arithmetic type
+// R (float, or a tangent number when the tangent-linear model differentiates
+// the step); with R = float they are the plain functors.
+
 // BounceBack<2>::apply(true,true) -- bbDomainBoundary.cuh:26-49
-__device__ __forceinline__ void bc_bounce_back(const Geometry& g, float f[9], int x, int y) {
+template <typename R>
+__device__ __forceinline__ void bc_bounce_back(const Geometry& g, R f[9], int x, int y) {
 #pragma unroll
     for (int i = 1; i < 9; i++) {
         int xn = x + CX(i), yn = y + CY(i);
@@ -241,35 +325,39 @@ __device__ __forceinline__ void bc_bounce_back(const Geometry& g, float f[9], in
 }
 
 // ZouHe::apply_top -- zouHeInflow.cuh:42-56
-__device__ __forceinline__ void bc_zouhe_top(float f[9], float ux) {
+template <typename R>
+__device__ __forceinline__ void bc_zouhe_top(R f[9], R ux) {
     const float uy = 0.0f;
-    float rho = (f[0] + f[1] + f[3] + 2.0f * (f[2] + f[5] + f[6])) / (1.0f + uy);
+    R rho = (f[0] + f[1] + f[3] + 2.0f * (f[2] + f[5] + f[6])) / (1.0f + uy);
     f[4] = f[2] - (2.0f / 3.0f) * rho * uy;
-    float d = f[1] - f[3];
+    R d = f[1] - f[3];
     f[7] = f[5] + 0.5f * d - 0.5f * rho * ux - (1.0f / 6.0f) * rho * uy;
     f[8] = f[6] - 0.5f * d + 0.5f * rho * ux - (1.0f / 6.0f) * rho * uy;
 }
 
 // ZouHe::apply_left -- zouHeInflow.cuh:9-22 (typo: f2 in the doubled term)
-__device__ __forceinline__ void bc_zouhe_left(float f[9], float ux, bool typo) {
-    float fin = typo ? f[2] : f[3];
-    float rho = (f[0] + f[2] + f[4] + 2.0f * (fin + f[6] + f[7])) / (1.0f - ux);
+template <typename R>
+__device__ __forceinline__ void bc_zouhe_left(R f[9], R ux, bool typo) {
+    R fin = typo ? f[2] : f[3];
+    R rho = (f[0] + f[2] + f[4] + 2.0f * (fin + f[6] + f[7])) / (1.0f - ux);
     f[1] = f[3] + (2.0f / 3.0f) * rho * ux;
     f[5] = f[7] - 0.5f * (f[2] - f[4]) + (1.0f / 6.0f) * rho * ux;
     f[8] = f[6] + 0.5f * (f[2] - f[4]) + (1.0f / 6.0f) * rho * ux;
 }
 
 // Zou-He pressure outlet at the right edge (no reference counterpart)
-__device__ __forceinline__ void bc_zouhe_pressure_right(float f[9], float rho) {
-    float ux = -1.0f + (f[0] + f[2] + f[4] + 2.0f * (f[1] + f[5] + f[8])) / rho;
+template <typename R>
+__device__ __forceinline__ void bc_zouhe_pressure_right(R f[9], float rho) {
+    R ux = -1.0f + (f[0] + f[2] + f[4] + 2.0f * (f[1] + f[5] + f[8])) / rho;
     f[3] = f[1] - (2.0f / 3.0f) * rho * ux;
     f[7] = f[5] + 0.5f * (f[2] - f[4]) - (1.0f / 6.0f) * rho * ux;
     f[6] = f[8] - 0.5f * (f[2] - f[4]) - (1.0f / 6.0f) * rho * ux;
 }
 
 // CylinderBoundary::apply -- cylinderBoundary.cuh:22-33 (full reversal)
-__device__ __forceinline__ void bc_cylinder(float f[9]) {
-    float s[9];
+template <typename R>
+__device__ __forceinline__ void bc_cylinder(R f[9]) {
+    R s[9];
 #pragma unroll
     for (int i = 0; i < 9; i++) s[i] = f[i];
 #pragma unroll
@@ -364,6 +452,14 @@ __device__ __forceinline__ void bc_reg_corner(const Geometry& g, float f[9], int
     }
 }
 
+// Parabolic inlet profile with peak u_bc over rows 0..ny-1 (no reference
+// counterpart: the reference's inlets are uniform)
+template <typename R>
+__device__ __forceinline__ R parabolic_ux(R u_bc, int y, int ny) {
+    const float h = (float)(ny - 1);
+    return 4.0f * u_bc * (float)y * (h - (float)y) / (h * h);
+}
+
 // Dispatch on the node's flag (boundaries_kernel_2D, boundaries.cuh:10-85).
 __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, int y, uint8_t fl) {
     const Geometry& g = a.g;
@@ -402,12 +498,7 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
             bc_reg_corner(g, f, x, y, a.aux[(long long)edge_index(x, y, g.nx, g.ny) * 9]);
         break;
     case LBMX_ZOU_HE_PRESSURE_RIGHT: bc_zouhe_pressure_right(f, a.rho_out_bc); break;
-    case LBMX_ZOU_HE_PARABOLIC_LEFT: {
-        float h = (float)(g.ny - 1);
-        float ux = 4.0f * a.u_bc * (float)y * (h - (float)y) / (h * h);
-        bc_zouhe_left(f, ux, false);
-        break;
-    }
+    case LBMX_ZOU_HE_PARABOLIC_LEFT: bc_zouhe_left(f, parabolic_ux(a.u_bc, y, g.ny), false); break;
     default: break;  // half-way walls act in load/store; unknown flags are left alone as the reference does
     }
 }

@@ -70,6 +70,12 @@ StepArgs base_args(const lbmx_handle* h);
 void set_step(const lbmx_handle* h, StepArgs& a, long long s);
 // 3-D tiled TMA descriptor over the population planes for tile_w x tile_h tiles
 bool encode_population_map(const lbmx_handle* h, CUtensorMap* out, int tile_w, int tile_h);
+// Peskin stencils of n markers (host array xy[2k], xy[2k+1]) on an nx x ny
+// lattice with row pitch `pitch`: sidx / sw [n][S*S] (S = 2 or 4) patch index
+// (-1 outside the lattice) and weight, nodes the patch's node offsets.
+// Returns -1, or the index of the first non-finite marker.
+int ibm_build_stencil(int nx, int ny, long long pitch, bool two_by_two, const float* xy, int n,
+                      std::vector<int>& sidx, std::vector<float>& sw, std::vector<int>& nodes);
 
 template <typename Fn>
 cudaError_t dispatch(int storage, Fn fn) {

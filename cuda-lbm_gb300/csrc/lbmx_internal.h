@@ -48,6 +48,8 @@ struct StepArgs {
     uint32_t quirks;
     int parity;              // step index & 1; 1 = neighbour-access phase
     int rest_plane;          // plane that holds f0 this step (0 or 9)
+    int sr;                  // 16-bit stores round stochastically (else to nearest)
+    uint32_t sr_seed;        // sr_seed_of(step index) for the rounding hash
     long long st_off[9];     // byte offset, from a node's plane-0 element, of the slot its q-th
                              // post-collision population goes to this step (interior nodes)
     float omega;
@@ -66,6 +68,12 @@ struct StepArgs {
     unsigned int* done_counter;        // CTAs finished in this launch
     int tile_chunk;                    // consecutive tiles taken per claim
 };
+
+// Seed of the stochastic-rounding hash for step index s (a Weyl sequence:
+// every step of a run gets a different seed).
+__host__ __device__ __forceinline__ uint32_t sr_seed_of(long long s) {
+    return (uint32_t)s * 0x9E3779B9u + 0x7F4A7C15u;
+}
 
 // perimeter index of a node on the domain edge
 __host__ __device__ inline int edge_index(int x, int y, int nx, int ny) {
@@ -93,21 +101,25 @@ cudaError_t launch_ibm_gather(const StepArgs& a, const int* patch_nodes, int npa
                               float* patch_rho, float* patch_u, cudaStream_t s);
 
 // IBM multi-direct forcing on the marker patch (lbmx_ibm.cu)
-struct IbmArgs {
+// The marker rounds' data; R is float for the engine and a tangent number
+// for the tangent-linear model.
+template <typename R>
+struct IbmData {
     int nm, npatch, iters, stencil;     // stencil: 2 or 4 nodes per axis
     const int* sten_idx;                // [nm][stencil^2] patch index or -1
     const float* sten_w;                // [nm][stencil^2] kernel weight
     const int* patch_nodes;             // [npatch] node offset (y*pitch + x)
-    const float* patch_rho;             // [npatch]
-    const float* patch_u;               // [2][npatch] uncorrected velocity
-    float* marker_u;                    // [2][nm] last interpolated velocity
-    float* marker_rho;                  // [nm]
-    float* marker_force;                // [2][nm] summed over iterations
-    float* ibm_force;                   // [2][plane] dense Eulerian force
+    const R* patch_rho;                 // [npatch]
+    const R* patch_u;                   // [2][npatch] uncorrected velocity
+    R* marker_u;                        // [2][nm] last interpolated velocity
+    R* marker_rho;                      // [nm]
+    R* marker_force;                    // [2][nm] summed over iterations
+    R* ibm_force;                       // [2][plane] dense Eulerian force
     long long plane;
     int clamp;
     float ds;
 };
+using IbmArgs = IbmData<float>;
 cudaError_t launch_ibm_iterate(const IbmArgs& a, cudaStream_t s);
 
 // Many lattices in one persistent launch (lbmx_batch.cu).  Work items are
@@ -122,6 +134,7 @@ struct BatchArgs {
     unsigned long long* counter;  // next item (reset by the last CTA)
     unsigned int* done;           // CTAs finished in this launch
     unsigned int* error_word;     // bit 1: a staging wait gave up
+    unsigned int* step;           // step index of this launch (for the rounding hash; the last CTA advances it)
 };
 // tile shape tile_w x tile_h: 64 x 8, 128 x 4 or 128 x 8; op: BGK, MRT or CM;
 // grid 0 only prepares the kernel (attributes) for a later graph capture

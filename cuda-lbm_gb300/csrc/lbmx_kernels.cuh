@@ -112,7 +112,7 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
 // code for boundary nodes, so a lattice gets bit-identical results from both
 // (inlined, the two callers may contract multiply-adds differently).
 template <typename T, int OP>
-__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[6]) {
+__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[6], uint32_t seed) {
     const long long off = (long long)y * a.g.pitch + x;
     float f[9];
     unsigned outmask;
@@ -167,7 +167,7 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v
         const float jmag = sqrtf(ux * ux + uy * uy) * rho;
         collide_cm<float>(f, rho, rho, ux, uy, Fx, Fy, a.S, optimal_rate<float>(rho, jmag, pimag, a.avg), true);
     }
-    store_post_collision<T>(a, x, y, f, outmask, fl);
+    store_post_collision<T>(a, x, y, f, outmask, fl, seed);
 }
 
 // ---------------------------------------------------------------- staging
@@ -285,7 +285,7 @@ __device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap
 // finite check (chosen at launch), so the unit is straight-line code.
 template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, bool LEAN = false>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
-                                              Acc v[6]) {
+                                              Acc v[6], uint32_t seed) {
     using St = Staging<T, TW, TH>;
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
@@ -357,14 +357,30 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     // slot q of the downstream nodes x + c_q (parity 1) or the nodes' own
     // slot OPP(q) (parity 0): byte offsets of this launch, from the host
     char* base = reinterpret_cast<char*>(F + off);
+    if (OFS && a.sr) {
+        // stochastic rounding, random bits from each node's hash
+        const uint32_t h0 = sr_hash((uint32_t)off >> 1, seed), h1 = sr_odd(h0);
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-        T* p = reinterpret_cast<T*>(base + a.st_off[q]);
-        if (P == 0 || CX(q) == 0) {
-            Store<T>::st2r(p, f[q].v);
-        } else {
-            Store<T>::str(p, f[q].v.x);
-            Store<T>::str(p + 1, f[q].v.y);
+        for (int q = 0; q < 9; q++) {
+            T* p = reinterpret_cast<T*>(base + a.st_off[q]);
+            const uint32_t r0 = sr_bits(h0, q), r1 = sr_bits(h1, q);
+            if (P == 0 || CX(q) == 0) {
+                Store<T>::st2r_sr(p, f[q].v, r0, r1);
+            } else {
+                Store<T>::str_sr(p, f[q].v.x, r0);
+                Store<T>::str_sr(p + 1, f[q].v.y, r1);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            T* p = reinterpret_cast<T*>(base + a.st_off[q]);
+            if (P == 0 || CX(q) == 0) {
+                Store<T>::st2r(p, f[q].v);
+            } else {
+                Store<T>::str(p, f[q].v.x);
+                Store<T>::str(p + 1, f[q].v.y);
+            }
         }
     }
 }
@@ -372,12 +388,12 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
 // One chunk of special nodes: consumer thread t takes node `first + t` of
 // the special-unit list (two nodes per unit).
 template <typename T, int OP>
-__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, Acc v[6]) {
+__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, Acc v[6], uint32_t seed) {
     const int k = chunk * kSpecialChunk + tid;
     if (k >= 2 * a.nspecial) return;
     const int off = a.special_units[k >> 1];
     const int y = off / a.g.pitch, x = off - y * a.g.pitch + (k & 1);
-    if (x < a.g.nx) general_node<T, OP>(a, x, y, v);
+    if (x < a.g.nx) general_node<T, OP>(a, x, y, v, seed);
 }
 
 template <typename T, int OP, int P, bool LEAN>
@@ -474,7 +490,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             const int4 sl = get_slot(&slot[s]);
             if (sl.x == -1) break;
             if (sl.x < 0) {
-                special_chunk<T, OP>(a, -2 - sl.x, tid, v);
+                special_chunk<T, OP>(a, -2 - sl.x, tid, v, a.sr_seed);
             } else {
                 const int x0 = sl.y + 2 * lx;
 #pragma unroll 1
@@ -487,7 +503,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                     }
                     if (live)
                         interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y,
-                                                              v);
+                                                              v, a.sr_seed);
                 }
             }
             __syncwarp();

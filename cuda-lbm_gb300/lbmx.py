@@ -24,6 +24,7 @@ MOVING_WALL_BB, ZOU_HE_PRESSURE_RIGHT, ZOU_HE_PARABOLIC_LEFT, HALFWAY_BB = 32, 3
 QUIRK_REST_LAG, QUIRK_ZOUHE_LEFT, QUIRK_MRT_FORCE, QUIRK_IBM_2X2, QUIRK_IBM_CLAMP = 1, 2, 4, 8, 16
 QUIRKS_REFERENCE = 0x1F
 OPTION_LAGGED_AVERAGES = 1
+OPTION_ROUND_NEAREST = 2
 STEP_STORE_MOMENTS, STEP_CHECK_FINITE, STEP_SUMS = 1, 2, 4
 
 STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INVALID_FLAGS",
@@ -38,7 +39,11 @@ EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy"
             "lbmx_batch_synchronize", "lbmx_batch_last_error", "lbmx_adjoint_create", "lbmx_adjoint_destroy",
             "lbmx_adjoint_set_state", "lbmx_adjoint_set_gamma", "lbmx_adjoint_set_scalars",
             "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward", "lbmx_adjoint_moments",
-            "lbmx_adjoint_last_error"]
+            "lbmx_adjoint_last_error", "lbmx_tangent_create", "lbmx_tangent_destroy", "lbmx_tangent_set_state",
+            "lbmx_tangent_set_markers", "lbmx_tangent_run", "lbmx_tangent_moments", "lbmx_tangent_time",
+            "lbmx_tangent_last_error"]
+# lbmx_tangent_create parameters
+TANGENT_U_BC, TANGENT_OMEGA, TANGENT_BODY_FX, TANGENT_WALL_UX = 0, 1, 2, 3
 
 
 class Params(ctypes.Structure):
@@ -127,6 +132,16 @@ def load_library(path=LIB_PATH):
     lib.lbmx_adjoint_moments.argtypes = [vp, vp, vp]
     lib.lbmx_adjoint_last_error.restype = ctypes.c_char_p
     lib.lbmx_adjoint_last_error.argtypes = [vp]
+    lib.lbmx_tangent_create.argtypes = [P(Params), vp, ctypes.c_int32, P(vp)]
+    lib.lbmx_tangent_destroy.argtypes = [vp]
+    lib.lbmx_tangent_set_state.argtypes = [vp, vp, vp]
+    lib.lbmx_tangent_set_markers.argtypes = [vp, vp, ctypes.c_int32]
+    lib.lbmx_tangent_run.argtypes = [vp, ctypes.c_int32, vp]
+    lib.lbmx_tangent_moments.argtypes = [vp, vp, vp, vp, vp]
+    lib.lbmx_tangent_time.restype = ctypes.c_int64
+    lib.lbmx_tangent_time.argtypes = [vp]
+    lib.lbmx_tangent_last_error.restype = ctypes.c_char_p
+    lib.lbmx_tangent_last_error.argtypes = [vp]
     for name in ("lbmx_adjoint_create", "lbmx_adjoint_set_state", "lbmx_adjoint_set_gamma", "lbmx_adjoint_set_scalars",
                  "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward",
                  "lbmx_adjoint_moments"):
@@ -402,3 +417,73 @@ class Adjoint:
         u = np.empty((2, self.ny, self.nx), np.float32)
         self._check(self.lib.lbmx_adjoint_moments(self.a, rho.ctypes.data, u.ctypes.data))
         return rho, u
+
+
+class Tangent:
+    """Tangent-linear derivative of a run with respect to one scalar parameter
+    (lbmx_tangent_*): TANGENT_U_BC, TANGENT_OMEGA, TANGENT_BODY_FX or
+    TANGENT_WALL_UX.  run() returns per step (drag, lift, d drag, d lift)."""
+
+    def __init__(self, nx, ny, parameter=TANGENT_U_BC, op=BGK, omega=1.0, S=None, periodic=(False, False),
+                 flags=None, quirks=0, u_bc=0.0, wall_u=(0.0, 0.0), rho_out=1.0, body_force=(0.0, 0.0),
+                 ibm_iters=3, device=0, stream=None):
+        self.lib = lib()
+        p = Params()
+        self.lib.lbmx_params_default(ctypes.byref(p))
+        p.nx, p.ny = nx, ny
+        p.periodic_x, p.periodic_y = int(bool(periodic[0])), int(bool(periodic[1]))
+        p.op, p.quirks, p.device, p.omega = op, quirks, device, omega
+        S = [omega] * 9 if S is None else S
+        for i in range(9):
+            p.S[i] = S[i]
+        p.u_bc, p.rho_out, p.ibm_iters = u_bc, rho_out, ibm_iters
+        p.wall_ux, p.wall_uy = wall_u
+        p.body_fx, p.body_fy = body_force
+        p.stream = stream
+        fl = np.zeros((ny, nx), np.uint8) if flags is None else np.ascontiguousarray(flags, np.uint8)
+        t = ctypes.c_void_p()
+        rc = self.lib.lbmx_tangent_create(ctypes.byref(p), fl.ctypes.data, int(parameter), ctypes.byref(t))
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_tangent_last_error(None).decode())
+        self.t = t
+        self.nx, self.ny, self.n = nx, ny, nx * ny
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LbmxError(rc, self.lib.lbmx_tangent_last_error(self.t).decode())
+
+    def close(self):
+        if getattr(self, "t", None):
+            self.lib.lbmx_tangent_destroy(self.t)
+            self.t = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, rho, u):
+        pr, k1 = _ptr(rho, np.float32)
+        pu, k2 = _ptr(u, np.float32)
+        self._check(self.lib.lbmx_tangent_set_state(self.t, pr, pu))
+
+    def set_markers(self, xy):
+        xy = np.ascontiguousarray(xy, np.float32).reshape(-1, 2)
+        self._check(self.lib.lbmx_tangent_set_markers(self.t, xy.ctypes.data, xy.shape[0]))
+
+    def run(self, nsteps):
+        series = np.zeros((int(nsteps), 4), np.float64)
+        self._check(self.lib.lbmx_tangent_run(self.t, int(nsteps), series.ctypes.data))
+        return series
+
+    def moments(self):
+        """(rho, u, drho, du) of the last step."""
+        rho = np.empty((self.ny, self.nx), np.float32)
+        u = np.empty((2, self.ny, self.nx), np.float32)
+        drho = np.empty_like(rho)
+        du = np.empty_like(u)
+        self._check(self.lib.lbmx_tangent_moments(self.t, rho.ctypes.data, u.ctypes.data, drho.ctypes.data,
+                                                  du.ctypes.data))
+        return rho, u, drho, du
+
+    @property
+    def t_steps(self):
+        return int(self.lib.lbmx_tangent_time(self.t))

@@ -82,7 +82,8 @@ enum {
 
 /* lbmx_params.options */
 enum {
-    LBMX_OPTION_LAGGED_AVERAGES = 1u << 0 /* CM_OPT: use the previous step's grid averages (one pass) */
+    LBMX_OPTION_LAGGED_AVERAGES = 1u << 0, /* CM_OPT: use the previous step's grid averages (one pass) */
+    LBMX_OPTION_ROUND_NEAREST = 1u << 1    /* 16-bit storage rounds to nearest instead of stochastically */
 };
 
 /* lbmx_step_ex flags */
@@ -273,6 +274,43 @@ lbmx_status lbmx_adjoint_backward(lbmx_adjoint* a, float* grad_gamma, double* gr
 /* rho[n], u[2n] of the last forward step */
 lbmx_status lbmx_adjoint_moments(lbmx_adjoint* a, float* rho, float* u);
 const char* lbmx_adjoint_last_error(lbmx_adjoint* a);
+
+/* ------------------------------------------------------------------ tangent
+ * No counterpart in the reference.  The tangent-linear (forward-mode)
+ * derivative of a run with respect to one scalar parameter: every value of
+ * the step carries its derivative through the same per-node boundary,
+ * collision and IBM code as the engine.  For one input this is the exact
+ * derivative of the discrete model that an adjoint would give, for every
+ * output at once -- the drag and lift of every step, the final moments --
+ * at the cost of one forward run and with no checkpoints.
+ * FP32 populations; BGK, MRT or CM; fluid, bounce-back, cylinder, Zou-He
+ * (top, left, parabolic left, pressure right) and half-way / moving walls;
+ * IBM markers; every quirk. */
+typedef struct lbmx_tangent lbmx_tangent;
+
+enum {
+    LBMX_TANGENT_U_BC = 0,    /* params.u_bc: Zou-He inlet velocity / parabolic peak */
+    LBMX_TANGENT_OMEGA = 1,   /* params.omega, with the S entries equal to it */
+    LBMX_TANGENT_BODY_FX = 2, /* params.body_fx */
+    LBMX_TANGENT_WALL_UX = 3  /* params.wall_ux of LBMX_MOVING_WALL_BB */
+};
+
+lbmx_status lbmx_tangent_create(const lbmx_params* p, const uint8_t* flags, int32_t parameter, lbmx_tangent** out);
+void lbmx_tangent_destroy(lbmx_tangent* t);
+/* initial rho[n], u[2n] (equilibrium populations, as lbmx_init_from_fields;
+ * the initial state does not depend on the parameter) */
+lbmx_status lbmx_tangent_set_state(lbmx_tangent* t, const float* rho, const float* u);
+/* IBM markers, as lbmx_ibm_set_markers */
+lbmx_status lbmx_tangent_set_markers(lbmx_tangent* t, const float* xy, int32_t n);
+/* nsteps further steps; series (may be NULL) receives per step
+ * {drag, lift, d drag / d parameter, d lift / d parameter}, drag and lift as
+ * lbmx_ibm_forces gives them */
+lbmx_status lbmx_tangent_run(lbmx_tangent* t, int32_t nsteps, double* series);
+/* rho[n], u[2n] of the last step and their derivatives drho[n], du[2n]
+ * (any may be NULL) */
+lbmx_status lbmx_tangent_moments(lbmx_tangent* t, float* rho, float* u, float* drho, float* du);
+int64_t lbmx_tangent_time(lbmx_tangent* t);
+const char* lbmx_tangent_last_error(lbmx_tangent* t);
 
 /* ------------------------------------------------------------------ batches
  * No counterpart in the reference, which runs one lattice per process

@@ -21,7 +21,10 @@ import pytest
 
 import oracle as O
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz")))
+# the reference build's dumps (the steady-state field of make_steady_cavity.py
+# is the FP64 oracle's and has its own test)
+GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz"))
+                if not os.path.basename(p).startswith("steady_"))
 TOL = 5e-6
 
 
