@@ -106,8 +106,6 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.tiles_y = h->tiles_y;
     a.num_ctas = h->num_ctas;
     a.error_word = h->error_word;
-    a.tile_counter = h->tile_counter;
-    a.done_counter = h->done_counter;
     a.tile_chunk = h->tile_chunk;
     a.sr = (h->p.storage != LBMX_STORAGE_F32 && !(h->p.options & LBMX_OPTION_ROUND_NEAREST)) ? 1 : 0;
     return a;
@@ -169,9 +167,10 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     // large lattices, still one item at a time on small ones
     h->tile_chunk = (int)std::max<long long>(1, items / (16LL * h->num_ctas));
     if (!h->partials) {
-        // the six FP64 grid accumulators (zero between launches)
-        LBMX_CUDA(h, cudaMalloc((void**)&h->partials, 8 * sizeof(double)));
-        LBMX_CUDA(h, cudaMemset(h->partials, 0, 8 * sizeof(double)));
+        // two sets (one per step parity) of kSumSlots copies of the six
+        // fixed-point grid accumulators (zero between uses)
+        LBMX_CUDA(h, cudaMalloc((void**)&h->partials, (size_t)2 * kAccPerSet * sizeof(double)));
+        LBMX_CUDA(h, cudaMemset(h->partials, 0, (size_t)2 * kAccPerSet * sizeof(double)));
     }
     return LBMX_OK;
 }
@@ -194,6 +193,9 @@ void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.parity = (int)(s & 1);
     a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? (a.parity ? 9 : 0) : 0;
     a.sr_seed = sr_seed_of(s);
+    // two work counters, alternating by step: each launch zeroes the other
+    a.tile_counter = h->tile_counter + (s & 1);
+    a.tile_counter_next = h->tile_counter + ((s + 1) & 1);
     // interior store targets: parity 1 -> slot q of the node x + c_q,
     // parity 0 -> the node's own slot OPP(q) (D2Q9 order: rest, E, N, W, S, NE, NW, SW, SE)
     static const int cx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
@@ -244,7 +246,7 @@ void lbmx_destroy(lbmx_handle* h) {
     cudaFree(h->force); cudaFree(h->gamma); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
     cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums);
     cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
-    cudaFree(h->tile_counter); cudaFree(h->done_counter);
+    cudaFree(h->tile_counter);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     cudaSetDevice(cur);
     delete h;
@@ -307,8 +309,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     ALLOC(h->sums, 6 * sizeof(double));
     ALLOC(h->avg, 3 * sizeof(float));
     ALLOC(h->error_word, sizeof(unsigned int));
-    ALLOC(h->tile_counter, sizeof(unsigned long long));
-    ALLOC(h->done_counter, sizeof(unsigned int));
+    ALLOC(h->tile_counter, 2 * sizeof(unsigned long long));
 #undef ALLOC
     if (p->stream) {
         h->stream = (cudaStream_t)p->stream;
@@ -324,8 +325,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     cudaMemsetAsync(h->sums, 0, 6 * sizeof(double), h->stream);
     cudaMemsetAsync(h->avg, 0, 3 * sizeof(float), h->stream);
     cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream);
-    cudaMemsetAsync(h->tile_counter, 0, sizeof(unsigned long long), h->stream);
-    cudaMemsetAsync(h->done_counter, 0, sizeof(unsigned int), h->stream);
+    cudaMemsetAsync(h->tile_counter, 0, 2 * sizeof(unsigned long long), h->stream);
     cudaMemsetAsync(h->aux, 0, (size_t)g.perimeter * 9 * sizeof(float), h->stream);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
         fail(nullptr, LBMX_ERR_CUDA, "lbmx_create: initial clears failed");
@@ -469,6 +469,8 @@ lbmx_status lbmx_init_from_fields(lbmx_handle* h, const float* rho, const float*
               }));
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
     h->t = 0;
+    h->last_step = -2;
+    h->pend_acc = h->pend_series3 = nullptr;
     h->initialized = true;
     h->have_avg = false;
     return LBMX_OK;
@@ -482,6 +484,11 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
     set_step(h, a, s);
     cudaStream_t st = h->stream;
     const int storage = h->p.storage;
+    // this step's work counter was zeroed by the previous launch, unless that
+    // was not this handle's previous step (a fresh state, batched steps)
+    if (h->last_step != s - 1)
+        LBMX_CUDA(h, cudaMemsetAsync(h->tile_counter, 0, 2 * sizeof(unsigned long long), st));
+    double* acc = h->partials + (size_t)(s & 1) * kAccPerSet;
     if (h->has_aux_bc)
         LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_edge_prepass<decltype(tag)>(a, h->aux, st); }));
     if (h->nm > 0) {
@@ -511,7 +518,7 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
     const bool lagged = opt && (h->p.options & LBMX_OPTION_LAGGED_AVERAGES) && h->have_avg;
     if (opt && !lagged) {
         StepArgs b = a;
-        b.partials = h->partials;
+        b.partials = acc;
         b.counter = h->counter;
         b.sums = nullptr;
         b.avg_out = h->avg;
@@ -523,7 +530,7 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
         a.u_out = h->u_out;
     }
     if (store || lagged || sums) {
-        a.partials = h->partials;
+        a.partials = acc;
         a.counter = h->counter;
         a.sums = (store || sums) ? h->sums : nullptr;
         // lagged CM_OPT: the averages of this step feed the next one
@@ -531,8 +538,28 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
     }
     a.check_finite = check ? 1 : 0;
     a.series3 = series3;
+    // the previous step's sums, if it left them to this launch
+    if (h->pend_acc) {
+        a.pub_acc = h->pend_acc;
+        a.pub_sums = h->sums;
+        a.pub_series3 = h->pend_series3;
+        h->pend_acc = h->pend_series3 = nullptr;
+    }
     LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->tmap, h->p.op, st); }));
+    if (step_mode(a) == kModeSums) {
+        h->pend_acc = acc;
+        h->pend_series3 = series3;
+    }
+    h->last_step = s;
     h->t = s;
+    return LBMX_OK;
+}
+
+// Publish sums a step left to the next launch when no step follows.
+static lbmx_status flush_sums(lbmx_handle* h) {
+    if (!h->pend_acc) return LBMX_OK;
+    LBMX_CUDA(h, launch_publish(h->pend_acc, h->sums, h->pend_series3, h->stream));
+    h->pend_acc = h->pend_series3 = nullptr;
     return LBMX_OK;
 }
 
@@ -549,6 +576,8 @@ lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags) {
             run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, (flags & LBMX_STEP_SUMS) != 0);
         if (st != LBMX_OK) return st;
     }
+    lbmx_status fs = flush_sums(h);
+    if (fs != LBMX_OK) return fs;
     if (check) {
         unsigned int w = 0;
         LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
@@ -581,10 +610,14 @@ lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, doubl
         lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, true,
                                   direct ? dev_series + 3 * (size_t)i : nullptr);
         if (st != LBMX_OK) return st;
-        if (!direct)
+        if (!direct) {
+            if ((st = flush_sums(h)) != LBMX_OK) return st;
             LBMX_CUDA(h, cudaMemcpyAsync(series + 3 * (size_t)i, h->sums, 3 * sizeof(double), cudaMemcpyDefault,
                                          h->stream));
+        }
     }
+    lbmx_status fs = flush_sums(h);
+    if (fs != LBMX_OK) return fs;
     if (check) {
         unsigned int w = 0;
         LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
@@ -874,6 +907,8 @@ lbmx_status lbmx_checkpoint_load(lbmx_handle* h, const char* path) {
     LBMX_CUDA(h, cudaMemcpy(h->edge, edge.data(), edge.size(), cudaMemcpyHostToDevice));
     LBMX_CUDA(h, cudaMemcpy(h->avg, avg, sizeof(avg), cudaMemcpyHostToDevice));
     h->t = hd.t;
+    h->last_step = -2;
+    h->pend_acc = h->pend_series3 = nullptr;
     h->initialized = true;
     h->have_avg = h->p.op == LBMX_CM_OPT && hd.t > 0;
     return LBMX_OK;

@@ -95,8 +95,7 @@ static lbmx_status refresh(lbmx_batch* b) {
         a.tiles_y = (h->g.ny - 2 + th - 1) / th;
         a.special_chunks = 0;
         a.num_ctas = 0;
-        a.tile_counter = nullptr;
-        a.done_counter = nullptr;
+        a.tile_counter = a.tile_counter_next = nullptr;
         // whole-struct memcpy keeps the (zeroed) padding, so the memcmp below
         // sees only real changes
         for (int v = 0; v < kVariants; v++)

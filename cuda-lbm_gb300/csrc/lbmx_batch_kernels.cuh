@@ -111,11 +111,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
                     }
                     if (live)
-                        interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v,
+                        interior_unit<T, OP, P, TW, TH, LEAN ? kModeLean : kModeFull>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y, v,
                                                               seed);
                 }
             } else {
-                special_chunk<T, OP>(a, -2 - sl.x, tid, v, seed);
+                special_chunk<T, OP, LEAN ? kModeLean : kModeFull>(a, -2 - sl.x, tid, v, seed);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);

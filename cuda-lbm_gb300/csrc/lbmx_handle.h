@@ -27,7 +27,7 @@ struct lbmx_handle {
     float* u_out = nullptr;        // [2][plane]
     float* staging = nullptr;      // dense [3][n] upload / readback staging
     float* pop_out = nullptr;      // dense [9][n] readback staging
-    double* partials = nullptr;    // [6] FP64 grid accumulators of the step's sums
+    double* partials = nullptr;    // [2][kAccPerSet] fixed-point grid accumulators of the step's sums
     unsigned int* counter = nullptr;
     double* sums = nullptr;        // [6]
     float* avg = nullptr;          // [3]
@@ -53,8 +53,10 @@ struct lbmx_handle {
     uint32_t* special_bits = nullptr;
     int nspecial = 0, special_chunks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
     void* f_alloc = nullptr;  // population allocation including the guard elements
-    unsigned long long* tile_counter = nullptr;
-    unsigned int* done_counter = nullptr;
+    unsigned long long* tile_counter = nullptr;  // [2] work counters, alternating by step
+    long long last_step = -2;      // step index of the last single-lattice launch
+    double* pend_acc = nullptr;    // accumulators of a step whose sums are not yet published
+    double* pend_series3 = nullptr;
     int tile_chunk = 1;
     CUtensorMap tmap;  // the type carries the 64-byte alignment TMA needs  // TMA descriptor of the population planes
     long long partial_cap = 0;

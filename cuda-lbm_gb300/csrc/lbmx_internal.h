@@ -64,9 +64,15 @@ struct StepArgs {
     const uint32_t* special_bits;  // 1 bit per unit for special units off the perimeter, or nullptr
     int tiles_x, tiles_y;          // interior tiles (kStageW x kStageH nodes, rows 1..ny-2)
     int num_ctas;                  // persistent CTAs that walk the interior tiles
-    unsigned long long* tile_counter;  // next interior tile to claim (reset by the last CTA)
-    unsigned int* done_counter;        // CTAs finished in this launch
+    unsigned long long* tile_counter;       // next work item to claim (this step's of two counters)
+    unsigned long long* tile_counter_next;  // the other counter: zeroed at the start for the next step
     int tile_chunk;                    // consecutive tiles taken per claim
+    // sums of the previous step left for this launch to publish (kModeSums
+    // steps publish one launch late; see step_mode): accumulators, the
+    // six-entry sums array, the series entry or null
+    double* pub_acc;
+    double* pub_sums;
+    double* pub_series3;
 };
 
 // Seed of the stochastic-rounding hash for step index s (a Weyl sequence:
@@ -147,6 +153,29 @@ cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w
 // kernel also runs 64 x 8 and 128 x 8 tiles.
 constexpr int kStepThreads = 288;  // 8 consumer warps + 1 producer warp
 constexpr int kConsumerWarps = 8;
+// Grid sums go into kSumSlots copies of the six fixed-point accumulators
+// (warp w of CTA b adds to slot (9 b + w) % kSumSlots), so few warps contend
+// for one address; a handle holds two such sets, one per step parity.
+constexpr int kSumSlots = 32;
+constexpr int kAccPerSet = kSumSlots * 6;
+
+// Interior-path variant of a step launch:
+//   kModeLean  no per-node force or Brinkman field, no moment store, no sums,
+//              no finite check -- straight-line code;
+//   kModeSums  the lean path plus the mass / momentum sums, published by the
+//              next launch on the stream (or lbmx's publish kernel), so the
+//              step itself ends with no fence or counter;
+//   kModeFull  everything, decided per launch from the arguments; the last
+//              CTA publishes its own sums.
+constexpr int kModeLean = 0, kModeSums = 1, kModeFull = 2;
+inline int step_mode(const StepArgs& a) {
+    const bool plain = !a.force && !a.gamma && !a.rho_out && !a.check_finite;
+    if (plain && !a.partials) return kModeLean;
+    if (plain && !a.avg_out) return kModeSums;
+    return kModeFull;
+}
+// publishes the sums in acc (one accumulator set) into sums / series3
+cudaError_t launch_publish(double* acc, double* sums, double* series3, cudaStream_t s);
 constexpr int kCtasPerSm = 3;      // resident persistent CTAs per SM (72 registers per thread)
 constexpr int kStageW = 128;
 constexpr int kStageH = 4;

@@ -41,14 +41,13 @@ using Acc = long long;
 constexpr float kFixScale = 1073741824.0f;  // 2^30
 __device__ __forceinline__ Acc fix(float t) { return __float2ll_rn(t * kFixScale); }
 
-// Grid reduction of the accumulators; the last CTA to finish publishes the
-// sums (sums, series, averages) and zeroes the accumulators for the next launch.
-__device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], long long n_nodes) {
-    __shared__ bool is_last;
+// A warp's totals of the first nsum accumulators into its slot.
+__device__ __forceinline__ void warp_sums(double* partials, const Acc v[6], int nsum) {
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int lane = tid & 31;
-    const int nsum = a.avg_out ? 6 : 3;
-    unsigned long long* acc = reinterpret_cast<unsigned long long*>(a.partials);
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nwarps = (blockDim.x * blockDim.y + 31) >> 5;
+    unsigned long long* acc =
+        reinterpret_cast<unsigned long long*>(partials) + ((blockIdx.x * nwarps + warp) % kSumSlots) * 6;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
         if (k >= nsum) break;
@@ -57,6 +56,40 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], lo
         for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
         if (lane == 0 && t != 0) atomicAdd(acc + k, (unsigned long long)t);
     }
+}
+
+// The first nsum sums of an accumulator set (integer sums over the slots:
+// the same bits in any order), zeroing the set for its next use.
+__device__ __forceinline__ void collect_sums(double* partials, int nsum, double s[6]) {
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials);
+    for (int k = 0; k < 6; k++) s[k] = 0.0;
+    for (int k = 0; k < nsum; k++) {
+        unsigned long long t = 0;
+        for (int j = 0; j < kSumSlots; j++) {
+            t += __ldcg(acc + j * 6 + k);
+            acc[j * 6 + k] = 0ull;
+        }
+        s[k] = (double)(long long)t * (1.0 / (double)kFixScale);
+    }
+}
+
+// Publish a kModeSums step's sums (one thread).
+__device__ __forceinline__ void publish_sums(double* partials, double* sums, double* series3) {
+    double s[6];
+    collect_sums(partials, 3, s);
+    if (sums)
+        for (int k = 0; k < 6; k++) sums[k] = s[k];
+    if (series3)
+        for (int k = 0; k < 3; k++) series3[k] = s[k];
+}
+
+// Grid reduction of the accumulators; the last CTA to finish publishes the
+// sums (sums, series, averages) and zeroes the accumulators for the next launch.
+__device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], long long n_nodes) {
+    __shared__ bool is_last;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nsum = a.avg_out ? 6 : 3;
+    warp_sums(a.partials, v, nsum);
     __syncthreads();
     if (tid == 0) {
         __threadfence();
@@ -66,11 +99,8 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], lo
     __syncthreads();
     if (!is_last || tid != 0) return;
     __threadfence();
-    double s[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < nsum; k++) {
-        s[k] = (double)(long long)__ldcg(acc + k) * (1.0 / (double)kFixScale);
-        acc[k] = 0ull;
-    }
+    double s[6];
+    collect_sums(a.partials, nsum, s);
     if (a.sums)
         for (int k = 0; k < 6; k++) a.sums[k] = s[k];
     if (a.series3)
@@ -280,10 +310,11 @@ __device__ __forceinline__ void stage_issue(const StepArgs& a, const CUtensorMap
     tma_load_3d(buf + (size_t)q * St::SLAB, tmap, x0 - St::A, y0 + dy, plane, bar);
 }
 
+// accumulators an interior-path variant (step_mode) touches
+__host__ __device__ constexpr int mode_sums(int mode) { return mode == kModeLean ? 0 : (mode == kModeSums ? 3 : 6); }
+
 // Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
-// LEAN: no per-node force or Brinkman field, no moment store, no sums, no
-// finite check (chosen at launch), so the unit is straight-line code.
-template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, bool LEAN = false>
+template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, int MODE = kModeFull>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
                                               Acc v[6], uint32_t seed) {
     using St = Staging<T, TW, TH>;
@@ -308,42 +339,44 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     const V2 jx = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
     const V2 jy = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
     V2 Fx = {make_float2(a.body_fx, a.body_fx)}, Fy = {make_float2(a.body_fy, a.body_fy)};
-    if (!LEAN && a.force) {
+    if (MODE == kModeFull && a.force) {
         Fx.v = *reinterpret_cast<const float2*>(a.force + off);
         Fy.v = *reinterpret_cast<const float2*>(a.force + plane + off);
     }
     const V2 inv = vdiv(splat(1.0f, rho), rho);
     V2 ux = fma(0.5f * Fx, inv, jx * inv);
     V2 uy = fma(0.5f * Fy, inv, jy * inv);
-    if (!LEAN && a.gamma) brinkman<V2>(V2{*reinterpret_cast<const float2*>(a.gamma + off)}, rho, ux, uy, Fx, Fy);
+    if (MODE == kModeFull && a.gamma) brinkman<V2>(V2{*reinterpret_cast<const float2*>(a.gamma + off)}, rho, ux, uy, Fx, Fy);
     V2 pimag = splat(0.f, rho);
-    if (OP == LBMX_CM_OPT || (!LEAN && a.partials && a.avg_out)) {
+    if (OP == LBMX_CM_OPT || (MODE == kModeFull && a.partials && a.avg_out)) {
         // offset form: sum c_x^2 w = sum c_y^2 w = 1/3
         const V2 d = OFS ? (f[5] + f[6]) + ((f[7] + f[8]) + splat(1.0f / 3.0f, rho)) : (f[5] + f[6]) + (f[7] + f[8]);
         const V2 pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
         const V2 pxy = (f[5] + f[7]) - (f[6] + f[8]);
         pimag = vsqrt(fma(pxx, pxx, fma(2.0f * pxy, pxy, pyy * pyy)));
     }
-    if (!LEAN && a.rho_out) {
+    if (MODE == kModeFull && a.rho_out) {
         *reinterpret_cast<float2*>(a.rho_out + off) = rho.v;
         *reinterpret_cast<float2*>(a.u_out + off) = ux.v;
         *reinterpret_cast<float2*>(a.u_out + plane + off) = uy.v;
     }
-    if (!LEAN && a.partials) {
-        // both nodes' terms in fixed point; the averages' terms only when
-        // averages are produced
+    if (MODE == kModeSums || (MODE == kModeFull && a.partials)) {
+        // the unit's terms in fixed point, the two nodes' summed in FP32
+        // first (a fixed pairing, so the sums stay the same bit for bit):
+        // half the 64-bit conversions, which run on the narrow FP64 pipe;
+        // the averages' terms only when averages are produced
         const V2 jx2 = rho * ux, jy2 = rho * uy;
-        v[0] += fix(rho.v.x) + fix(rho.v.y);
-        v[1] += fix(jx2.v.x) + fix(jx2.v.y);
-        v[2] += fix(jy2.v.x) + fix(jy2.v.y);
-        if (a.avg_out) {
+        v[0] += fix(rho.v.x + rho.v.y);
+        v[1] += fix(jx2.v.x + jx2.v.y);
+        v[2] += fix(jy2.v.x + jy2.v.y);
+        if (MODE == kModeFull && a.avg_out) {
             v[3] += fix(rho.v.x) + fix(rho.v.y);
             v[4] += fix(rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x)) +
                     fix(rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y));
             v[5] += fix(pimag.v.x) + fix(pimag.v.y);
         }
     }
-    if (!LEAN && a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
+    if (MODE == kModeFull && a.check_finite && !(isfinite(rho.v.x) && isfinite(rho.v.y))) atomicOr(a.error_word, 1u);
     if (OP == LBMX_BGK) {
         collide_bgk<V2, OFS>(f, rho, drho, ux, uy, Fx, Fy, a.omega, a.forced);
     } else if (OP == LBMX_MRT) {
@@ -387,16 +420,23 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
 
 // One chunk of special nodes: consumer thread t takes node `first + t` of
 // the special-unit list (two nodes per unit).
-template <typename T, int OP>
+template <typename T, int OP, int MODE = kModeFull>
 __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, Acc v[6], uint32_t seed) {
     const int k = chunk * kSpecialChunk + tid;
     if (k >= 2 * a.nspecial) return;
     const int off = a.special_units[k >> 1];
     const int y = off / a.g.pitch, x = off - y * a.g.pitch + (k & 1);
-    if (x < a.g.nx) general_node<T, OP>(a, x, y, v, seed);
+    if (x >= a.g.nx) return;
+    // the out-of-line call gets its own accumulators, so the caller's stay
+    // in registers
+    Acc t[6] = {0, 0, 0, 0, 0, 0};
+    general_node<T, OP>(a, x, y, t, seed);
+    if (mode_sums(MODE) > 0 && a.partials)
+#pragma unroll
+        for (int k = 0; k < mode_sums(MODE); k++) v[k] += t[k];
 }
 
-template <typename T, int OP, int P, bool LEAN>
+template <typename T, int OP, int P, int MODE>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
     constexpr int TW = step_tile_w((int)sizeof(T)), TH = step_tile_h((int)sizeof(T));
     // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
@@ -424,6 +464,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             mbar_init(&empty[s], kConsumerWarps);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (blockIdx.x == 0) {
+            // the next step's work counter (the previous launch used it and
+            // has finished), and the previous step's sums if it left them
+            *a.tile_counter_next = 0ull;
+            if (a.pub_acc) publish_sums(a.pub_acc, a.pub_sums, a.pub_series3);
+        }
     }
     __syncthreads();
     if (warp == kConsumerWarps) {
@@ -490,7 +536,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             const int4 sl = get_slot(&slot[s]);
             if (sl.x == -1) break;
             if (sl.x < 0) {
-                special_chunk<T, OP>(a, -2 - sl.x, tid, v, a.sr_seed);
+                special_chunk<T, OP, MODE>(a, -2 - sl.x, tid, v, a.sr_seed);
             } else {
                 const int x0 = sl.y + 2 * lx;
 #pragma unroll 1
@@ -502,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
                     }
                     if (live)
-                        interior_unit<T, OP, P, TW, TH, LEAN>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y,
+                        interior_unit<T, OP, P, TW, TH, MODE>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y,
                                                               v, a.sr_seed);
                 }
             }
@@ -510,17 +556,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             if (lane == 0) mbar_arrive(&empty[s]);
         }
     }
-    if (a.partials) block_sums(a, v, (long long)a.g.nx * a.g.ny);
-    // the last CTA to finish re-arms the item counter for the next launch
-    if (tid == 0) {
-        __threadfence();
-        if (atomicAdd(a.done_counter, 1u) == gridDim.x - 1) {
-            *a.tile_counter = 0ull;
-            *a.done_counter = 0u;
-            __threadfence();
-        }
-    }
+    // kModeSums: each warp adds its totals and is done (the next launch
+    // publishes them); kModeFull: the last CTA publishes
+    if (MODE == kModeSums) warp_sums(a.partials, v, 3);
+    else if (MODE == kModeFull && a.partials) block_sums(a, v, (long long)a.g.nx * a.g.ny);
 }
+
 
 // Grid averages <rho>, <rho |u|>, <|Pi|> of the current step before any
 // collision (update_avg_mag, macroscopics.cuh:50-120), for CM_OPT.
@@ -707,7 +748,7 @@ __global__ void ibm_gather_kernel(const StepArgs a, const int* patch_nodes, int 
     pu[npatch + i] = jy * inv;
 }
 
-template <typename T, int OP, int P, bool LEAN>
+template <typename T, int OP, int P, int MODE>
 static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tmap, unsigned grid, cudaStream_t s) {
     // the staged ring needs more than the default 48 KB; set once per device
     static unsigned long long configured = 0;
@@ -715,21 +756,23 @@ static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tma
     cudaGetDevice(&dev);
     if (!(configured >> (dev & 63) & 1ull)) {
         cudaError_t e = cudaFuncSetAttribute(
-            step_kernel<T, OP, P, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            step_kernel<T, OP, P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
             (int)Staging<T, step_tile_w((int)sizeof(T)), step_tile_h((int)sizeof(T))>::SMEM);
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    step_kernel<T, OP, P, LEAN>
+    step_kernel<T, OP, P, MODE>
         <<<grid, kThreads, Staging<T, step_tile_w((int)sizeof(T)), step_tile_h((int)sizeof(T))>::SMEM, s>>>(a, tmap);
     return cudaGetLastError();
 }
 
 template <typename T, int OP, int P>
 static cudaError_t launch_step_lean(const StepArgs& a, const CUtensorMap& tmap, unsigned grid, cudaStream_t s) {
-    const bool lean = !a.force && !a.gamma && !a.rho_out && !a.partials && !a.check_finite;
-    return lean ? launch_step_variant<T, OP, P, true>(a, tmap, grid, s)
-                : launch_step_variant<T, OP, P, false>(a, tmap, grid, s);
+    switch (step_mode(a)) {
+    case kModeLean: return launch_step_variant<T, OP, P, kModeLean>(a, tmap, grid, s);
+    case kModeSums: return launch_step_variant<T, OP, P, kModeSums>(a, tmap, grid, s);
+    default: return launch_step_variant<T, OP, P, kModeFull>(a, tmap, grid, s);
+    }
 }
 
 template <typename T>
