@@ -21,6 +21,8 @@
 // AA pattern makes every population slot the property of one node, so the
 // two sets of CTAs never write the same memory.
 #pragma once
+#include <cstring>
+
 #include "lbmx_device.cuh"
 
 namespace lbmx {
@@ -464,12 +466,20 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             mbar_init(&empty[s], kConsumerWarps);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if (blockIdx.x == 0) {
-            // the next step's work counter (the previous launch used it and
-            // has finished), and the previous step's sums if it left them
-            *a.tile_counter_next = 0ull;
-            if (a.pub_acc) publish_sums(a.pub_acc, a.pub_sums, a.pub_series3);
-        }
+    }
+    // Programmatic dependent launch: this grid may have started while the
+    // previous step's grid was still draining.  Wait for that grid to finish
+    // (its writes are then visible) before touching anything it wrote, then
+    // let the next step's grid start its own prologue: every CTA of this grid
+    // is resident by now, so the waiting grid cannot hold SM slots this one
+    // still needs.  Without the launch attribute both are no-ops.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" :::);
+    if (tid == 0 && blockIdx.x == 0) {
+        // the next step's work counter (the previous launch used it and has
+        // finished), and the previous step's sums if it left them
+        *a.tile_counter_next = 0ull;
+        if (a.pub_acc) publish_sums(a.pub_acc, a.pub_sums, a.pub_series3);
     }
     __syncthreads();
     if (warp == kConsumerWarps) {
@@ -761,9 +771,21 @@ static cudaError_t launch_step_variant(const StepArgs& a, const CUtensorMap& tma
         if (e != cudaSuccess) return e;
         configured |= 1ull << (dev & 63);
     }
-    step_kernel<T, OP, P, MODE>
-        <<<grid, kThreads, Staging<T, step_tile_w((int)sizeof(T)), step_tile_h((int)sizeof(T))>::SMEM, s>>>(a, tmap);
-    return cudaGetLastError();
+    // launched with programmatic stream serialization: a step that directly
+    // follows another overlaps its launch and prologue with that one's tail
+    // (the kernel waits on griddepcontrol.wait before its first dependent access)
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = Staging<T, step_tile_w((int)sizeof(T)), step_tile_h((int)sizeof(T))>::SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, step_kernel<T, OP, P, MODE>, a, tmap);
 }
 
 template <typename T, int OP, int P>
