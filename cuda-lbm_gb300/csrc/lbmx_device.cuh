@@ -138,6 +138,10 @@ template <> struct Store<float> {
         *reinterpret_cast<float2*>(p) = v;
     }
     static __device__ __forceinline__ void st_sr(float* p, float v, float, uint32_t) { *p = v; }
+    // two consecutive values at any (element-aligned) address
+    static __device__ __forceinline__ float2 ld2r_u(const float* p) { return make_float2(p[0], p[1]); }
+    static __device__ __forceinline__ void st2r_u(float* p, float2 v) { p[0] = v.x; p[1] = v.y; }
+    static __device__ __forceinline__ void st2r_sr_u(float* p, float2 v, uint32_t, uint32_t) { p[0] = v.x; p[1] = v.y; }
 };
 template <> struct Store<__half> {
     static constexpr float kUp = 4096.0f, kDown = 1.0f / 4096.0f;  // 2^12 storage scale
@@ -162,6 +166,22 @@ template <> struct Store<__half> {
         *reinterpret_cast<__half2*>(p) = __float22half2_rn(make_float2(sr_cut16(s.x, r0), sr_cut16(s.y, r1)));
     }
     static __device__ __forceinline__ void st_sr(__half* p, float v, float w, uint32_t r) { str_sr(p, v - w, r); }
+    // two consecutive values at any (element-aligned) address: converted and
+    // scaled as a pair, moved as two halves
+    static __device__ __forceinline__ float2 ld2r_u(const __half* p) {
+        return __fmul2_rn(__half22float2(__halves2half2(p[0], p[1])), make_float2(kDown, kDown));
+    }
+    static __device__ __forceinline__ void st2r_u(__half* p, float2 v) {
+        const __half2 h = __float22half2_rn(__fmul2_rn(v, make_float2(kUp, kUp)));
+        p[0] = __low2half(h);
+        p[1] = __high2half(h);
+    }
+    static __device__ __forceinline__ void st2r_sr_u(__half* p, float2 v, uint32_t r0, uint32_t r1) {
+        const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
+        const __half2 h = __float22half2_rn(make_float2(sr_cut16(s.x, r0), sr_cut16(s.y, r1)));
+        p[0] = __low2half(h);
+        p[1] = __high2half(h);
+    }
 };
 template <> struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ float ldr(const __nv_bfloat16* p) { return __bfloat162float(*p); }
@@ -188,6 +208,21 @@ template <> struct Store<__nv_bfloat16> {
     }
     static __device__ __forceinline__ void st_sr(__nv_bfloat16* p, float v, float w, uint32_t r) {
         str_sr(p, v - w, r);
+    }
+    static __device__ __forceinline__ float2 ld2r_u(const __nv_bfloat16* p) {
+        return __bfloat1622float2(__halves2bfloat162(p[0], p[1]));
+    }
+    static __device__ __forceinline__ void st2r_u(__nv_bfloat16* p, float2 v) {
+        const __nv_bfloat162 h = __float22bfloat162_rn(v);
+        p[0] = __low2bfloat16(h);
+        p[1] = __high2bfloat16(h);
+    }
+    static __device__ __forceinline__ void st2r_sr_u(__nv_bfloat16* p, float2 v, uint32_t r0, uint32_t r1) {
+        __nv_bfloat16_raw lo, hi;
+        lo.x = (unsigned short)(sr_bf16_bits(v.x, r0) >> 16);
+        hi.x = (unsigned short)(sr_bf16_bits(v.y, r1) >> 16);
+        p[0] = __nv_bfloat16(lo);
+        p[1] = __nv_bfloat16(hi);
     }
 };
 

@@ -332,8 +332,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     for (int q = 0; q < 9; q++) {
         const bool shifted = P && CX(q) != 0;
         const T* s = sbuf + q * St::SLAB + r * St::TWP + 2 * lx + (shifted ? St::A - CX(q) : St::A);
-        if (shifted) f[q].v = make_float2(Store<T>::ldr(s), Store<T>::ldr(s + 1));
-        else f[q].v = Store<T>::ld2r(s);
+        f[q].v = shifted ? Store<T>::ld2r_u(s) : Store<T>::ld2r(s);
     }
     V2 rho = ((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7])) + f[8];
     const V2 drho = rho;                     // offset form: rho - 1, exactly
@@ -399,23 +398,15 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         for (int q = 0; q < 9; q++) {
             T* p = reinterpret_cast<T*>(base + a.st_off[q]);
             const uint32_t r0 = sr_bits(h0, q), r1 = sr_bits(h1, q);
-            if (P == 0 || CX(q) == 0) {
-                Store<T>::st2r_sr(p, f[q].v, r0, r1);
-            } else {
-                Store<T>::str_sr(p, f[q].v.x, r0);
-                Store<T>::str_sr(p + 1, f[q].v.y, r1);
-            }
+            if (P == 0 || CX(q) == 0) Store<T>::st2r_sr(p, f[q].v, r0, r1);
+            else Store<T>::st2r_sr_u(p, f[q].v, r0, r1);
         }
     } else {
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             T* p = reinterpret_cast<T*>(base + a.st_off[q]);
-            if (P == 0 || CX(q) == 0) {
-                Store<T>::st2r(p, f[q].v);
-            } else {
-                Store<T>::str(p, f[q].v.x);
-                Store<T>::str(p + 1, f[q].v.y);
-            }
+            if (P == 0 || CX(q) == 0) Store<T>::st2r(p, f[q].v);
+            else Store<T>::st2r_u(p, f[q].v);
         }
     }
 }
