@@ -255,7 +255,11 @@ __device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y
     const bool edge = on_edge(g, x, y);
     const bool hw = is_halfway(fl);
     const float* E = a.edge + ((long long)a.parity * g.perimeter + (edge ? edge_index(x, y, g.nx, g.ny) : 0)) * 9;
+    // Every source address is chosen by selects, always in bounds, and all
+    // loads are issued before any value is used: a node's nine loads are in
+    // flight together instead of one after another behind branches.
     unsigned m = 0;
+    const T* src[9];
 #pragma unroll
     for (int q = 1; q < 9; q++) {
         int sx = x - CX(q), sy = y - CY(q);
@@ -268,19 +272,22 @@ __device__ __forceinline__ void load_post_stream(const StepArgs& a, int x, int y
             if (g.periodic_y) sy = sy < 0 ? sy + g.ny : sy - g.ny;
             else out = true;
         }
-        if (out) {
-            m |= 1u << q;
-            if (hw) {
-                const float v = Store<T>::ld(F + q * g.plane + row + x, WQ(q));
-                f[q] = a.parity ? v - wall_term(a, OPP(q), fl) : v;
-            } else {
-                f[q] = E[q];
-            }
-        } else if (a.parity) {
-            f[q] = Store<T>::ld(F + OPP(q) * g.plane + (long long)sy * g.pitch + sx, WQ(q));
-        } else {
-            f[q] = Store<T>::ld(F + q * g.plane + row + x, WQ(q));
-        }
+        if (out) m |= 1u << q;
+        // the node's own slot q (parity 0, or a half-way node's reflection),
+        // else slot OPP(q) of the upstream node
+        src[q] = (out || !a.parity) ? F + q * g.plane + row + x
+                                    : F + OPP(q) * g.plane + (long long)sy * g.pitch + sx;
+    }
+    float vs[9], es[9];
+#pragma unroll
+    for (int q = 1; q < 9; q++) {
+        vs[q] = Store<T>::ld(src[q], WQ(q));
+        es[q] = ((m >> q) & 1u) && !hw ? E[q] : 0.0f;
+    }
+#pragma unroll
+    for (int q = 1; q < 9; q++) {
+        if ((m >> q) & 1u) f[q] = hw ? (a.parity ? vs[q] - wall_term(a, OPP(q), fl) : vs[q]) : es[q];
+        else f[q] = vs[q];
     }
     *outmask = m;
 }
