@@ -104,6 +104,7 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.special_bits = h->special_bits;
     a.tiles_x = h->tiles_x;
     a.tiles_y = h->tiles_y;
+    a.hw_cols = h->hw_cols;
     a.num_ctas = h->num_ctas;
     a.error_word = h->error_word;
     a.tile_chunk = h->tile_chunk;
@@ -153,6 +154,25 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     }
     h->nspecial = (int)units.size();
     h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
+    // columns of half-way / moving walls with fluid beside them (the right
+    // one as the second node of full units, so nx even), no IBM patch node
+    // in their units
+    h->hw_cols = 0;
+    if (!h->flags_host.empty() && !g.periodic_x && g.nx >= 4 && g.ny >= 3) {
+        auto flag = [&](int x, int y) { return h->flags_host[(size_t)y * g.pitch + x]; };
+        auto wall = [](uint8_t f) { return f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB; };
+        bool left = true, right = (g.nx % 2) == 0;
+        for (int y = 1; y < g.ny - 1; y++) {
+            left = left && wall(flag(0, y)) && flag(1, y) == LBMX_FLUID;
+            right = right && wall(flag(g.nx - 1, y)) && flag(g.nx - 2, y) == LBMX_FLUID;
+        }
+        for (int off : h->patch_host) {
+            const int x = off % g.pitch;
+            if (x <= 1) left = false;
+            if (x >= g.nx - 2) right = false;
+        }
+        h->hw_cols = (left ? 1 : 0) | (right ? 2 : 0);
+    }
     const int es = (int)elem_size(h->p.storage);
     h->tiles_x = (g.nx + step_tile_w(es) - 1) / step_tile_w(es);
     h->tiles_y = (g.ny - 2 + step_tile_h(es) - 1) / step_tile_h(es);

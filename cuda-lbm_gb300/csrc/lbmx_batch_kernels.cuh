@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
 #pragma unroll
                 for (int r = r0; r < TH; r += St::ROWS) {
                     const int y = sl.z + r;
-                    bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
+                    bool live = y < a.g.ny - 1 && (x0 > 0 || (P == 0 && (a.hw_cols & 1))) &&
+                                (x0 + 1 < a.g.nx - 1 || (P == 0 && (a.hw_cols & 2) && x0 + 2 == a.g.nx));
                     if (live && a.special_bits) {
                         const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;

@@ -52,6 +52,7 @@ struct lbmx_handle {
     int* special_units = nullptr;
     uint32_t* special_bits = nullptr;
     int nspecial = 0, special_chunks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
+    int hw_cols = 0;                  // StepArgs::hw_cols
     void* f_alloc = nullptr;  // population allocation including the guard elements
     unsigned long long* tile_counter = nullptr;  // [2] work counters, alternating by step
     long long last_step = -2;      // step index of the last single-lattice launch

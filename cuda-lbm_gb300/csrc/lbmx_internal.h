@@ -63,6 +63,11 @@ struct StepArgs {
     int special_chunks;            // work items of kSpecialChunk special nodes that lead the work list
     const uint32_t* special_bits;  // 1 bit per unit for special units off the perimeter, or nullptr
     int tiles_x, tiles_y;          // interior tiles (kStageW x kStageH nodes, rows 1..ny-2)
+    // bit 0 / bit 1: the left / right column (rows 1..ny-2) is all half-way
+    // or moving walls with fluid beside it.  In an own-node step (parity 0)
+    // such a wall node reads and writes only its own slots, exactly as an
+    // interior node does, so the tiles take those units then.
+    int hw_cols;
     int num_ctas;                  // persistent CTAs that walk the interior tiles
     unsigned long long* tile_counter;       // next work item to claim (this step's of two counters)
     unsigned long long* tile_counter_next;  // the other counter: zeroed at the start for the next step

@@ -418,8 +418,12 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
     const int k = chunk * kSpecialChunk + tid;
     if (k >= 2 * a.nspecial) return;
     const int off = a.special_units[k >> 1];
-    const int y = off / a.g.pitch, x = off - y * a.g.pitch + (k & 1);
+    const int y = off / a.g.pitch, x0 = off - y * a.g.pitch, x = x0 + (k & 1);
     if (x >= a.g.nx) return;
+    // wall columns the tiles take in an own-node step
+    if (a.parity == 0 && a.hw_cols && y > 0 && y < a.g.ny - 1 &&
+        ((x0 == 0 && (a.hw_cols & 1)) || (x0 + 2 == a.g.nx && (a.hw_cols & 2))))
+        return;
     // the out-of-line call gets its own accumulators, so the caller's stay
     // in registers
     Acc t[6] = {0, 0, 0, 0, 0, 0};
@@ -543,7 +547,8 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
 #pragma unroll 1
                 for (int r = r0; r < TH; r += St::ROWS) {
                     const int y = sl.z + r;
-                    bool live = y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1;
+                    bool live = y < a.g.ny - 1 && (x0 > 0 || (P == 0 && (a.hw_cols & 1))) &&
+                                (x0 + 1 < a.g.nx - 1 || (P == 0 && (a.hw_cols & 2) && x0 + 2 == a.g.nx));
                     if (live && a.special_bits) {
                         const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;

@@ -143,3 +143,19 @@ def test_single_steps_around_batched_steps(storage):
     a.step(1, flags=lbmx.STEP_SUMS)
     b.step(9)
     assert np.array_equal(np.nan_to_num(a.populations()), np.nan_to_num(b.populations()))
+
+
+@pytest.mark.parametrize("storage", [0, 1, 2])
+@pytest.mark.parametrize("nx", [96, 99])
+def test_sums_match_the_stored_moments(storage, nx):
+    # widths short of a whole tile: the sums must cover exactly the lattice's
+    # nodes (tile lanes past the edge hold no nodes), in both step parities
+    c = C.random_state(C.cavity_moving_wall(nx, 70, op=C.MRT), seed=10)
+    L = C.make_lattice(c, storage=storage)
+    for k in (3, 4):
+        L.step(1 if k == 4 else 3)
+        rho, u, s = L.moments()
+        r64 = rho.astype(np.float64)
+        assert abs(s[0] - r64.sum()) <= 1e-9 * r64.sum()
+        assert abs(s[1] - (r64 * u[0]).sum()) <= 1e-6 * np.abs(r64 * u[0]).sum()
+        assert abs(s[2] - (r64 * u[1]).sum()) <= 1e-6 * np.abs(r64 * u[1]).sum()
