@@ -156,6 +156,8 @@ def test_sums_match_the_stored_moments(storage, nx):
         L.step(1 if k == 4 else 3)
         rho, u, s = L.moments()
         r64 = rho.astype(np.float64)
-        assert abs(s[0] - r64.sum()) <= 1e-9 * r64.sum()
+        # fixed-point terms of 2^-30; interior units add their two nodes in
+        # FP32 first (one rounding of about 1e-7 per pair)
+        assert abs(s[0] - r64.sum()) <= 2e-7 * r64.sum()
         assert abs(s[1] - (r64 * u[0]).sum()) <= 1e-6 * np.abs(r64 * u[0]).sum()
         assert abs(s[2] - (r64 * u[1]).sum()) <= 1e-6 * np.abs(r64 * u[1]).sum()
