@@ -104,7 +104,6 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.special_bits = h->special_bits;
     a.tiles_x = h->tiles_x;
     a.tiles_y = h->tiles_y;
-    a.hw_cols = h->hw_cols;
     a.num_ctas = h->num_ctas;
     a.error_word = h->error_word;
     a.tile_chunk = h->tile_chunk;
@@ -130,8 +129,21 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
             for (int x = 0; x < g.nx; x++)
                 if (h->flags_host[(size_t)y * g.pitch + x]) mark((long long)y * g.pitch + x);
     for (int off : h->patch_host) mark(off);
-    std::vector<int> units;
-    std::vector<uint32_t> bits(((size_t)g.ny * units_per_row + 31) / 32, 0u);
+    // an own-node step (parity 0) runs a node through the tiles unless it has
+    // a boundary functor, an IBM patch force or (fluid on a non-periodic
+    // edge) reads the edge store
+    std::vector<char> patch((size_t)g.plane, 0);
+    for (int off : h->patch_host) patch[(size_t)off] = 1;
+    auto plain0 = [&](int x, int y) {
+        const size_t off = (size_t)y * g.pitch + x;
+        if (patch[off]) return false;
+        const uint8_t f = h->flags_host.empty() ? (uint8_t)LBMX_FLUID : h->flags_host[off];
+        if (f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB) return true;
+        const bool edge = (!g.periodic_x && (x == 0 || x == g.nx - 1)) || (!g.periodic_y && (y == 0 || y == g.ny - 1));
+        return f == LBMX_FLUID && !edge;
+    };
+    std::vector<int> units, units0;
+    std::vector<uint32_t> bits(((size_t)g.ny * units_per_row + 31) / 32, 0u), bits0(bits.size(), 0u);
     for (int y = 0; y < g.ny; y++)
         for (int x0 = 0; x0 < g.nx; x0 += 2) {
             const bool perim = y == 0 || y == g.ny - 1 || x0 == 0 || x0 + 1 >= g.nx - 1;
@@ -141,41 +153,36 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
                 bits[u >> 5] |= 1u << (u & 31);
                 any_interior = true;
             }
+            if (x0 + 1 >= g.nx || !plain0(x0, y) || !plain0(x0 + 1, y)) {
+                units0.push_back(y * g.pitch + x0);
+                bits0[u >> 5] |= 1u << (u & 31);
+            }
         }
     cudaFree(h->special_units);
     cudaFree(h->special_bits);
-    h->special_units = nullptr;
-    h->special_bits = nullptr;
-    LBMX_CUDA(h, cudaMalloc((void**)&h->special_units, units.size() * sizeof(int)));
+    cudaFree(h->special_units0);
+    cudaFree(h->special_bits0);
+    h->special_units = h->special_units0 = nullptr;
+    h->special_bits = h->special_bits0 = nullptr;
+    LBMX_CUDA(h, cudaMalloc((void**)&h->special_units, std::max<size_t>(1, units.size()) * sizeof(int)));
     LBMX_CUDA(h, cudaMemcpy(h->special_units, units.data(), units.size() * sizeof(int), cudaMemcpyHostToDevice));
     if (any_interior) {
         LBMX_CUDA(h, cudaMalloc((void**)&h->special_bits, bits.size() * sizeof(uint32_t)));
         LBMX_CUDA(h, cudaMemcpy(h->special_bits, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
+    LBMX_CUDA(h, cudaMalloc((void**)&h->special_units0, std::max<size_t>(1, units0.size()) * sizeof(int)));
+    if (!units0.empty()) {
+        LBMX_CUDA(h, cudaMemcpy(h->special_units0, units0.data(), units0.size() * sizeof(int), cudaMemcpyHostToDevice));
+        LBMX_CUDA(h, cudaMalloc((void**)&h->special_bits0, bits0.size() * sizeof(uint32_t)));
+        LBMX_CUDA(h, cudaMemcpy(h->special_bits0, bits0.data(), bits0.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
     h->nspecial = (int)units.size();
     h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
-    // columns of half-way / moving walls with fluid beside them (the right
-    // one as the second node of full units, so nx even), no IBM patch node
-    // in their units
-    h->hw_cols = 0;
-    if (!h->flags_host.empty() && !g.periodic_x && g.nx >= 4 && g.ny >= 3) {
-        auto flag = [&](int x, int y) { return h->flags_host[(size_t)y * g.pitch + x]; };
-        auto wall = [](uint8_t f) { return f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB; };
-        bool left = true, right = (g.nx % 2) == 0;
-        for (int y = 1; y < g.ny - 1; y++) {
-            left = left && wall(flag(0, y)) && flag(1, y) == LBMX_FLUID;
-            right = right && wall(flag(g.nx - 1, y)) && flag(g.nx - 2, y) == LBMX_FLUID;
-        }
-        for (int off : h->patch_host) {
-            const int x = off % g.pitch;
-            if (x <= 1) left = false;
-            if (x >= g.nx - 2) right = false;
-        }
-        h->hw_cols = (left ? 1 : 0) | (right ? 2 : 0);
-    }
+    h->nspecial0 = (int)units0.size();
+    h->special_chunks0 = (2 * h->nspecial0 + kSpecialChunk - 1) / kSpecialChunk;
     const int es = (int)elem_size(h->p.storage);
     h->tiles_x = (g.nx + step_tile_w(es) - 1) / step_tile_w(es);
-    h->tiles_y = (g.ny - 2 + step_tile_h(es) - 1) / step_tile_h(es);
+    h->tiles_y = (g.ny + step_tile_h(es) - 1) / step_tile_h(es);
     // persistent CTAs walk the work list: kCtasPerSm per SM on large
     // lattices; two per SM when each CTA would get fewer than 16 items (a
     // small lattice is latency-bound and gains more from fuller CTAs than
@@ -213,6 +220,11 @@ void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.parity = (int)(s & 1);
     a.rest_plane = (h->p.quirks & LBMX_QUIRK_REST_LAG) ? (a.parity ? 9 : 0) : 0;
     a.sr_seed = sr_seed_of(s);
+    // the general path's units of this parity
+    a.special_units = a.parity ? h->special_units : h->special_units0;
+    a.nspecial = a.parity ? h->nspecial : h->nspecial0;
+    a.special_chunks = a.parity ? h->special_chunks : h->special_chunks0;
+    a.special_bits = a.parity ? h->special_bits : h->special_bits0;
     // two work counters, alternating by step: each launch zeroes the other
     a.tile_counter = h->tile_counter + (s & 1);
     a.tile_counter_next = h->tile_counter + ((s + 1) & 1);
@@ -266,6 +278,7 @@ void lbmx_destroy(lbmx_handle* h) {
     cudaFree(h->force); cudaFree(h->gamma); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
     cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums);
     cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
+    cudaFree(h->special_units0); cudaFree(h->special_bits0);
     cudaFree(h->tile_counter);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     cudaSetDevice(cur);

@@ -30,8 +30,8 @@ struct lbmx_batch {
     // device state of the current configuration
     StepArgs* d_args = nullptr;        // [kVariants][2 parities][count]
     CUtensorMap* d_tmaps = nullptr;    // [count]
-    int2* d_items = nullptr;
-    int nitems = 0, items_cap = 0;
+    int2* d_items[2] = {nullptr, nullptr};  // work list of an own-node (0) and a neighbour-access (1) step
+    int nitems[2] = {0, 0}, items_cap[2] = {0, 0};
     unsigned long long* counter = nullptr;
     unsigned int* done = nullptr;
     unsigned int* error_word = nullptr;
@@ -92,7 +92,7 @@ static lbmx_status refresh(lbmx_batch* b) {
         const lbmx_handle* h = b->lat[l];
         StepArgs a = base_args(h);
         a.tiles_x = (h->g.nx + tw - 1) / tw;
-        a.tiles_y = (h->g.ny - 2 + th - 1) / th;
+        a.tiles_y = (h->g.ny + th - 1) / th;
         a.special_chunks = 0;
         a.num_ctas = 0;
         a.tile_counter = a.tile_counter_next = nullptr;
@@ -121,35 +121,40 @@ static lbmx_status refresh(lbmx_batch* b) {
     if (!b->d_args) BATCH_CUDA(b, cudaMalloc((void**)&b->d_args, args.size() * sizeof(StepArgs)));
     BATCH_CUDA(b, cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(StepArgs), cudaMemcpyHostToDevice,
                                   b->stream));
-    // TMA descriptors and the work list: special chunks of every lattice
-    // first (slower per unit), then each lattice's interior tiles
+    // TMA descriptors and, per parity, the work list: special chunks of every
+    // lattice first (slower per unit), then each lattice's tiles
     std::vector<CUtensorMap> maps(n);
-    std::vector<int2> items;
-    for (int l = 0; l < n; l++) {
+    for (int l = 0; l < n; l++)
         if (!encode_population_map(b->lat[l], &maps[l], tw, th))
             return bfail(b, LBMX_ERR_CUDA, "lbmx_batch: cannot build the TMA descriptor of lattice %d", l);
-        const int chunks = (2 * b->lat[l]->nspecial + kSpecialChunk - 1) / kSpecialChunk;
-        for (int c = 0; c < chunks; c++) items.push_back(make_int2(l, -(c + 1)));
-    }
-    for (int l = 0; l < n; l++) {
-        const StepArgs& a = args[l];
-        const long long tiles = (long long)a.tiles_x * a.tiles_y;
-        for (long long t = 0; t < tiles; t++) items.push_back(make_int2(l, (int)t));
-    }
-    if (items.size() > (size_t)0x7fffffff) return bfail(b, LBMX_ERR_TOO_LARGE, "lbmx_batch: too many work items");
     if (!b->d_tmaps) BATCH_CUDA(b, cudaMalloc((void**)&b->d_tmaps, (size_t)n * sizeof(CUtensorMap)));
     BATCH_CUDA(b, cudaMemcpyAsync(b->d_tmaps, maps.data(), (size_t)n * sizeof(CUtensorMap), cudaMemcpyHostToDevice,
                                   b->stream));
-    if ((int)items.size() > b->items_cap) {
-        cudaFree(b->d_items);
-        b->d_items = nullptr;
-        BATCH_CUDA(b, cudaMalloc((void**)&b->d_items, items.size() * sizeof(int2)));
-        b->items_cap = (int)items.size();
+    std::vector<int2> items[2];
+    for (int p = 0; p < 2; p++) {
+        for (int l = 0; l < n; l++) {
+            const int ns = p ? b->lat[l]->nspecial : b->lat[l]->nspecial0;
+            const int chunks = (2 * ns + kSpecialChunk - 1) / kSpecialChunk;
+            for (int c = 0; c < chunks; c++) items[p].push_back(make_int2(l, -(c + 1)));
+        }
+        for (int l = 0; l < n; l++) {
+            const StepArgs& a = args[l];
+            const long long tiles = (long long)a.tiles_x * a.tiles_y;
+            for (long long t = 0; t < tiles; t++) items[p].push_back(make_int2(l, (int)t));
+        }
+        if (items[p].size() > (size_t)0x7fffffff)
+            return bfail(b, LBMX_ERR_TOO_LARGE, "lbmx_batch: too many work items");
+        if ((int)items[p].size() > b->items_cap[p]) {
+            cudaFree(b->d_items[p]);
+            b->d_items[p] = nullptr;
+            BATCH_CUDA(b, cudaMalloc((void**)&b->d_items[p], items[p].size() * sizeof(int2)));
+            b->items_cap[p] = (int)items[p].size();
+        }
+        BATCH_CUDA(b, cudaMemcpyAsync(b->d_items[p], items[p].data(), items[p].size() * sizeof(int2),
+                                      cudaMemcpyHostToDevice, b->stream));
+        b->nitems[p] = (int)items[p].size();
     }
-    BATCH_CUDA(b, cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice,
-                                  b->stream));
     BATCH_CUDA(b, cudaStreamSynchronize(b->stream));
-    b->nitems = (int)items.size();
     b->host_args.swap(args);
     b->args_tile_w = tw;
     b->args_tile_h = th;
@@ -175,14 +180,14 @@ static lbmx_status launch_one(lbmx_batch* b, long long s, int variant) {
     BatchArgs ba;
     ba.lat = b->d_args + ((size_t)variant * 2 + parity) * n;
     ba.tmaps = b->d_tmaps;
-    ba.items = b->d_items;
-    ba.nitems = b->nitems;
+    ba.items = b->d_items[parity];
+    ba.nitems = b->nitems[parity];
     ba.chunk = b->cfg.chunk;
     ba.counter = b->counter;
     ba.done = b->done;
     ba.error_word = b->error_word;
     ba.step = b->step;
-    const unsigned grid = (unsigned)std::max(1, std::min(b->nitems, b->cfg.ctas_per_sm * b->num_sms));
+    const unsigned grid = (unsigned)std::max(1, std::min(b->nitems[parity], b->cfg.ctas_per_sm * b->num_sms));
     // plain steps of lattices without per-node force or Brinkman fields run
     // the kernel without those branches
     const bool lean = variant == 0 && b->lean;
@@ -294,7 +299,7 @@ void lbmx_batch_destroy(lbmx_batch* b) {
     if (b->own_stream && b->stream) cudaStreamSynchronize(b->stream);
     else cudaDeviceSynchronize();
     drop_graphs(b);
-    cudaFree(b->d_args); cudaFree(b->d_tmaps); cudaFree(b->d_items);
+    cudaFree(b->d_args); cudaFree(b->d_tmaps); cudaFree(b->d_items[0]); cudaFree(b->d_items[1]);
     cudaFree(b->counter); cudaFree(b->done); cudaFree(b->error_word); cudaFree(b->step);
     for (cudaEvent_t e : b->stream_events) cudaEventDestroy(e);
     if (b->end_event) cudaEventDestroy(b->end_event);

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
             }
             const StepArgs& a = b.lat[it.x];
             const int ty = it.y / a.tiles_x, tx = it.y - ty * a.tiles_x;
-            const int x0 = tx * TW, y0 = 1 + ty * TH;
+            const int x0 = tx * TW, y0 = ty * TH;
             if (lane == 0) {
                 put_slot(&slot[s], it.y, x0, y0, it.x);
                 fence_proxy_async_smem();
@@ -105,8 +105,10 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
 #pragma unroll
                 for (int r = r0; r < TH; r += St::ROWS) {
                     const int y = sl.z + r;
-                    bool live = y < a.g.ny - 1 && (x0 > 0 || (P == 0 && (a.hw_cols & 1))) &&
-                                (x0 + 1 < a.g.nx - 1 || (P == 0 && (a.hw_cols & 2) && x0 + 2 == a.g.nx));
+                    // parity 1: not on the perimeter; parity 0: both nodes in the
+                    // lattice; either way, not marked for the general path
+                    bool live = P ? (y > 0 && y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1)
+                                  : (y < a.g.ny && x0 + 1 < a.g.nx);
                     if (live && a.special_bits) {
                         const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;

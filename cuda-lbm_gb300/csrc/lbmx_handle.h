@@ -49,10 +49,14 @@ struct lbmx_handle {
     std::vector<int> patch_host;   // IBM patch node offsets
     // work split of the step kernel
     std::vector<uint8_t> flags_host;  // pitched copy of the flags (empty: all fluid)
+    // general-path units of a neighbour-access step (parity 1) and of an
+    // own-node step (parity 0)
     int* special_units = nullptr;
     uint32_t* special_bits = nullptr;
+    int* special_units0 = nullptr;
+    uint32_t* special_bits0 = nullptr;
+    int nspecial0 = 0, special_chunks0 = 0;
     int nspecial = 0, special_chunks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
-    int hw_cols = 0;                  // StepArgs::hw_cols
     void* f_alloc = nullptr;  // population allocation including the guard elements
     unsigned long long* tile_counter = nullptr;  // [2] work counters, alternating by step
     long long last_step = -2;      // step index of the last single-lattice launch

@@ -58,16 +58,19 @@ struct StepArgs {
     float body_fx, body_fy;
     int forced;              // any non-zero force (body, field or IBM)
     // work split of the step kernel (lbmx_kernels.cuh)
+    // The general path's units of this step (set_step picks the parity's):
+    // a neighbour-access step (parity 1) takes every perimeter unit (the
+    // tiles find them by position) and the units with a flagged or IBM-patch
+    // node (special_bits marks those off the perimeter); an own-node step
+    // (parity 0) only units with a boundary functor, an IBM patch node, a
+    // fluid node reading the edge store or a missing second node
+    // (special_bits marks them all) -- there a half-way or moving wall node
+    // reads and writes only its own slots, exactly as an interior node does.
     const int* special_units;      // unit offsets y*pitch + x0 handled by the general path
     int nspecial;
     int special_chunks;            // work items of kSpecialChunk special nodes that lead the work list
-    const uint32_t* special_bits;  // 1 bit per unit for special units off the perimeter, or nullptr
-    int tiles_x, tiles_y;          // interior tiles (kStageW x kStageH nodes, rows 1..ny-2)
-    // bit 0 / bit 1: the left / right column (rows 1..ny-2) is all half-way
-    // or moving walls with fluid beside it.  In an own-node step (parity 0)
-    // such a wall node reads and writes only its own slots, exactly as an
-    // interior node does, so the tiles take those units then.
-    int hw_cols;
+    const uint32_t* special_bits;  // 1 bit per unit (see above), or nullptr
+    int tiles_x, tiles_y;          // tiles of kStageW x kStageH nodes covering the lattice
     int num_ctas;                  // persistent CTAs that walk the interior tiles
     unsigned long long* tile_counter;       // next work item to claim (this step's of two counters)
     unsigned long long* tile_counter_next;  // the other counter: zeroed at the start for the next step

@@ -418,12 +418,8 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
     const int k = chunk * kSpecialChunk + tid;
     if (k >= 2 * a.nspecial) return;
     const int off = a.special_units[k >> 1];
-    const int y = off / a.g.pitch, x0 = off - y * a.g.pitch, x = x0 + (k & 1);
+    const int y = off / a.g.pitch, x = off - y * a.g.pitch + (k & 1);
     if (x >= a.g.nx) return;
-    // wall columns the tiles take in an own-node step
-    if (a.parity == 0 && a.hw_cols && y > 0 && y < a.g.ny - 1 &&
-        ((x0 == 0 && (a.hw_cols & 1)) || (x0 + 2 == a.g.nx && (a.hw_cols & 2))))
-        return;
     // the out-of-line call gets its own accumulators, so the caller's stay
     // in registers
     Acc t[6] = {0, 0, 0, 0, 0, 0};
@@ -514,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             }
             const int tile = item - nchunks;
             const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
-            const int x0 = tx * St::TW, y0 = 1 + ty * St::TH;
+            const int x0 = tx * St::TW, y0 = ty * St::TH;
             if (lane == 0) {
                 put_slot(&slot[s], tile, x0, y0, 0);
                 fence_proxy_async_smem();
@@ -547,8 +543,10 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
 #pragma unroll 1
                 for (int r = r0; r < TH; r += St::ROWS) {
                     const int y = sl.z + r;
-                    bool live = y < a.g.ny - 1 && (x0 > 0 || (P == 0 && (a.hw_cols & 1))) &&
-                                (x0 + 1 < a.g.nx - 1 || (P == 0 && (a.hw_cols & 2) && x0 + 2 == a.g.nx));
+                    // parity 1: not on the perimeter; parity 0: both nodes in the
+                    // lattice; either way, not marked for the general path
+                    bool live = P ? (y > 0 && y < a.g.ny - 1 && x0 > 0 && x0 + 1 < a.g.nx - 1)
+                                  : (y < a.g.ny && x0 + 1 < a.g.nx);
                     if (live && a.special_bits) {
                         const long long unit = ((long long)y * a.g.pitch + x0) >> 1;
                         live = ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) == 0;
