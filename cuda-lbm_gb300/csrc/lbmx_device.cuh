@@ -86,8 +86,9 @@ constexpr bool kOffset = sizeof(T) == 2;
 
 // 32 well-mixed bits of a unit (two x-neighbouring nodes, even offset) and
 // the step seed: the "lowbias32" integer finaliser (C. Wellons,
-// hash-prospector) of a Weyl-scrambled key.  The odd node of the unit
-// multiplies it by an odd constant.
+// hash-prospector) of a Weyl-scrambled key.  Each population's 32 random
+// bits (sr_bits) serve both nodes of the unit: bits 15:0 the even node,
+// bits 31:16 the odd one.
 __device__ __forceinline__ uint32_t sr_hash(uint32_t unit, uint32_t seed) {
     uint32_t h = unit * 0x9E3779B1u ^ seed;
     h ^= h >> 16;
@@ -97,32 +98,38 @@ __device__ __forceinline__ uint32_t sr_hash(uint32_t unit, uint32_t seed) {
     h ^= h >> 16;
     return h;
 }
-__device__ __forceinline__ uint32_t sr_odd(uint32_t h) { return h * 0xA24BAED5u; }
-__device__ __forceinline__ uint32_t sr_node_hash(uint32_t off, uint32_t seed) {
-    const uint32_t h = sr_hash(off >> 1, seed);
-    return (off & 1u) ? sr_odd(h) : h;
+// random bits of population q from a unit's hash: the product with an odd
+// constant per q (a bijection, so uniform), its high half folded into its
+// low half (again a bijection) -- otherwise the low half would depend on the
+// hash's low bits only and repeat its pattern across the populations
+__device__ __forceinline__ uint32_t sr_bits(uint32_t h, int q) {
+    const uint32_t r = h * (0x2545F491u + 0x9E3779B8u * (uint32_t)q);
+    return r ^ (r >> 16);
 }
-// random bits of population q from a node's hash: an odd multiplier per q
-// (a bijection of the 32-bit hash, whose top bits are then uniform)
-__device__ __forceinline__ uint32_t sr_bits(uint32_t h, int q) { return h * (0x2545F491u + 0x9E3779B8u * (uint32_t)q); }
 
-// Stochastic FP32 -> FP16 in two exact steps: 13 random bits added below
-// FP16's last mantissa bit, the 13 bits cleared, then a round-to-nearest
-// conversion that finds the value already representable (in FP16's normal
-// range) -- so overflow still gives Inf and NaN stays NaN, and two values
-// convert in one packed instruction.
-__device__ __forceinline__ float sr_cut16(float x, uint32_t r) {
-    return __uint_as_float((__float_as_uint(x) + (r >> 19)) & 0xFFFFE000u);
+// The conversions themselves are the hardware's (PTX cvt.rs, sm_100 and
+// later): two FP32 values to a packed pair, the upper element rounded with
+// random bits rbits[31:16], the lower with rbits[15:0] (the random bits are
+// added below the last kept bit, then the value is truncated).
+__device__ __forceinline__ uint32_t cvt_rs_f16x2(float hi, float lo, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
 }
-__device__ __forceinline__ __half sr_half(float x, uint32_t r) { return __float2half_rn(sr_cut16(x, r)); }
-// FP32 -> BF16: 16 random bits added below BF16's last mantissa bit, then
-// the high half of the word is the result (Inf + bits is NaN, NaN stays NaN)
-__device__ __forceinline__ uint32_t sr_bf16_bits(float x, uint32_t r) { return __float_as_uint(x) + (r >> 16); }
-__device__ __forceinline__ __nv_bfloat16 sr_bf16(float x, uint32_t r) {
-    __nv_bfloat16_raw b;
-    b.x = (unsigned short)(sr_bf16_bits(x, r) >> 16);
-    return __nv_bfloat16(b);
+__device__ __forceinline__ uint32_t cvt_rs_bf16x2(float hi, float lo, uint32_t rbits) {
+    uint32_t d;
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
 }
+// one value from the low half of a packed result; r16 in bits 15:0
+__device__ __forceinline__ unsigned short sr_half_bits(float x, uint32_t r16) {
+    return (unsigned short)(cvt_rs_f16x2(0.0f, x, r16) & 0xFFFFu);
+}
+__device__ __forceinline__ unsigned short sr_bf16_bits(float x, uint32_t r16) {
+    return (unsigned short)(cvt_rs_bf16x2(0.0f, x, r16) & 0xFFFFu);
+}
+// the 16 random bits of node `lane` (0: x0, 1: x0 + 1) of a unit's 32
+__device__ __forceinline__ uint32_t sr_lane16(uint32_t r, int lane) { return lane ? r >> 16 : r & 0xFFFFu; }
 
 template <> struct Store<float> {
     static __device__ __forceinline__ float ldr(const float* p) { return *p; }
@@ -134,14 +141,14 @@ template <> struct Store<float> {
     static __device__ __forceinline__ float2 ld2(const float* p, float) { return *reinterpret_cast<const float2*>(p); }
     static __device__ __forceinline__ void st2(float* p, float2 v, float) { *reinterpret_cast<float2*>(p) = v; }
     static __device__ __forceinline__ void str_sr(float* p, float v, uint32_t) { *p = v; }
-    static __device__ __forceinline__ void st2r_sr(float* p, float2 v, uint32_t, uint32_t) {
+    static __device__ __forceinline__ void st2r_sr(float* p, float2 v, uint32_t) {
         *reinterpret_cast<float2*>(p) = v;
     }
     static __device__ __forceinline__ void st_sr(float* p, float v, float, uint32_t) { *p = v; }
     // two consecutive values at any (element-aligned) address
     static __device__ __forceinline__ float2 ld2r_u(const float* p) { return make_float2(p[0], p[1]); }
     static __device__ __forceinline__ void st2r_u(float* p, float2 v) { p[0] = v.x; p[1] = v.y; }
-    static __device__ __forceinline__ void st2r_sr_u(float* p, float2 v, uint32_t, uint32_t) { p[0] = v.x; p[1] = v.y; }
+    static __device__ __forceinline__ void st2r_sr_u(float* p, float2 v, uint32_t) { p[0] = v.x; p[1] = v.y; }
 };
 template <> struct Store<__half> {
     static constexpr float kUp = 4096.0f, kDown = 1.0f / 4096.0f;  // 2^12 storage scale
@@ -160,12 +167,15 @@ template <> struct Store<__half> {
         return make_float2(d.x + w, d.y + w);
     }
     static __device__ __forceinline__ void st2(__half* p, float2 v, float w) { st2r(p, make_float2(v.x - w, v.y - w)); }
-    static __device__ __forceinline__ void str_sr(__half* p, float v, uint32_t r) { *p = sr_half(v * kUp, r); }
-    static __device__ __forceinline__ void st2r_sr(__half* p, float2 v, uint32_t r0, uint32_t r1) {
-        const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
-        *reinterpret_cast<__half2*>(p) = __float22half2_rn(make_float2(sr_cut16(s.x, r0), sr_cut16(s.y, r1)));
+    // r16: 16 random bits (bits 15:0); r: a pair's 32
+    static __device__ __forceinline__ void str_sr(__half* p, float v, uint32_t r16) {
+        *reinterpret_cast<unsigned short*>(p) = sr_half_bits(v * kUp, r16);
     }
-    static __device__ __forceinline__ void st_sr(__half* p, float v, float w, uint32_t r) { str_sr(p, v - w, r); }
+    static __device__ __forceinline__ void st2r_sr(__half* p, float2 v, uint32_t r) {
+        const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
+        *reinterpret_cast<uint32_t*>(p) = cvt_rs_f16x2(s.y, s.x, r);
+    }
+    static __device__ __forceinline__ void st_sr(__half* p, float v, float w, uint32_t r16) { str_sr(p, v - w, r16); }
     // two consecutive values at any (element-aligned) address: converted and
     // scaled as a pair, moved as two halves
     static __device__ __forceinline__ float2 ld2r_u(const __half* p) {
@@ -176,11 +186,11 @@ template <> struct Store<__half> {
         p[0] = __low2half(h);
         p[1] = __high2half(h);
     }
-    static __device__ __forceinline__ void st2r_sr_u(__half* p, float2 v, uint32_t r0, uint32_t r1) {
+    static __device__ __forceinline__ void st2r_sr_u(__half* p, float2 v, uint32_t r) {
         const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
-        const __half2 h = __float22half2_rn(make_float2(sr_cut16(s.x, r0), sr_cut16(s.y, r1)));
-        p[0] = __low2half(h);
-        p[1] = __high2half(h);
+        const uint32_t d = cvt_rs_f16x2(s.y, s.x, r);
+        reinterpret_cast<unsigned short*>(p)[0] = (unsigned short)(d & 0xFFFFu);
+        reinterpret_cast<unsigned short*>(p)[1] = (unsigned short)(d >> 16);
     }
 };
 template <> struct Store<__nv_bfloat16> {
@@ -201,13 +211,14 @@ template <> struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ void st2(__nv_bfloat16* p, float2 v, float w) {
         *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn(make_float2(v.x - w, v.y - w));
     }
-    static __device__ __forceinline__ void str_sr(__nv_bfloat16* p, float v, uint32_t r) { *p = sr_bf16(v, r); }
-    static __device__ __forceinline__ void st2r_sr(__nv_bfloat16* p, float2 v, uint32_t r0, uint32_t r1) {
-        // the two high halves in one word
-        *reinterpret_cast<uint32_t*>(p) = __byte_perm(sr_bf16_bits(v.x, r0), sr_bf16_bits(v.y, r1), 0x7632);
+    static __device__ __forceinline__ void str_sr(__nv_bfloat16* p, float v, uint32_t r16) {
+        *reinterpret_cast<unsigned short*>(p) = sr_bf16_bits(v, r16);
     }
-    static __device__ __forceinline__ void st_sr(__nv_bfloat16* p, float v, float w, uint32_t r) {
-        str_sr(p, v - w, r);
+    static __device__ __forceinline__ void st2r_sr(__nv_bfloat16* p, float2 v, uint32_t r) {
+        *reinterpret_cast<uint32_t*>(p) = cvt_rs_bf16x2(v.y, v.x, r);
+    }
+    static __device__ __forceinline__ void st_sr(__nv_bfloat16* p, float v, float w, uint32_t r16) {
+        str_sr(p, v - w, r16);
     }
     static __device__ __forceinline__ float2 ld2r_u(const __nv_bfloat16* p) {
         return __bfloat1622float2(__halves2bfloat162(p[0], p[1]));
@@ -217,12 +228,10 @@ template <> struct Store<__nv_bfloat16> {
         p[0] = __low2bfloat16(h);
         p[1] = __high2bfloat16(h);
     }
-    static __device__ __forceinline__ void st2r_sr_u(__nv_bfloat16* p, float2 v, uint32_t r0, uint32_t r1) {
-        __nv_bfloat16_raw lo, hi;
-        lo.x = (unsigned short)(sr_bf16_bits(v.x, r0) >> 16);
-        hi.x = (unsigned short)(sr_bf16_bits(v.y, r1) >> 16);
-        p[0] = __nv_bfloat16(lo);
-        p[1] = __nv_bfloat16(hi);
+    static __device__ __forceinline__ void st2r_sr_u(__nv_bfloat16* p, float2 v, uint32_t r) {
+        const uint32_t d = cvt_rs_bf16x2(v.y, v.x, r);
+        reinterpret_cast<unsigned short*>(p)[0] = (unsigned short)(d & 0xFFFFu);
+        reinterpret_cast<unsigned short*>(p)[1] = (unsigned short)(d >> 16);
     }
 };
 
@@ -305,10 +314,12 @@ __device__ __forceinline__ void store_post_collision(const StepArgs& a, int x, i
     const long long row = (long long)y * g.pitch;
     const bool hw = is_halfway(fl);
     const bool sr = kOffset<T> && a.sr;
-    const uint32_t h = sr ? sr_node_hash((uint32_t)(row + x), seed) : 0u;
-    // the value f of population q goes to p, rounded as configured
+    const uint32_t h = sr ? sr_hash((uint32_t)(row + x) >> 1, seed) : 0u;
+    const int lane = (int)((row + x) & 1);
+    // the value f of population q goes to p, rounded as configured (the
+    // node's half of its unit's random bits)
     auto put = [&](T* p, float v, int q) {
-        if (sr) Store<T>::st_sr(p, v, WQ(q), sr_bits(h, q));
+        if (sr) Store<T>::st_sr(p, v, WQ(q), sr_lane16(sr_bits(h, q), lane));
         else Store<T>::st(p, v, WQ(q));
     };
     put(F + a.rest_plane * g.plane + row + x, f[0], 0);

@@ -393,13 +393,13 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     char* base = reinterpret_cast<char*>(F + off);
     if (OFS && a.sr) {
         // stochastic rounding, random bits from each node's hash
-        const uint32_t h0 = sr_hash((uint32_t)off >> 1, seed), h1 = sr_odd(h0);
+        const uint32_t h = sr_hash((uint32_t)off >> 1, seed);
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             T* p = reinterpret_cast<T*>(base + a.st_off[q]);
-            const uint32_t r0 = sr_bits(h0, q), r1 = sr_bits(h1, q);
-            if (P == 0 || CX(q) == 0) Store<T>::st2r_sr(p, f[q].v, r0, r1);
-            else Store<T>::st2r_sr_u(p, f[q].v, r0, r1);
+            const uint32_t r = sr_bits(h, q);
+            if (P == 0 || CX(q) == 0) Store<T>::st2r_sr(p, f[q].v, r);
+            else Store<T>::st2r_sr_u(p, f[q].v, r);
         }
     } else {
 #pragma unroll
