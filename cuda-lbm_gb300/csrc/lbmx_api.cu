@@ -864,7 +864,7 @@ static uint32_t crc32_update(uint32_t crc, const void* data, size_t n) {
 }
 
 struct CheckpointHeader {
-    char magic[8];  // "LBMXCKP1"
+    char magic[8];  // "LBMXCKP2"
     int32_t nx, ny, pitch, nplanes, storage, op, periodic_x, periodic_y;
     uint32_t quirks, reserved;
     int64_t t;
@@ -877,7 +877,7 @@ lbmx_status lbmx_checkpoint_save(lbmx_handle* h, const char* path) {
     cudaSetDevice(h->p.device);
     CheckpointHeader hd;
     memset(&hd, 0, sizeof(hd));
-    memcpy(hd.magic, "LBMXCKP1", 8);
+    memcpy(hd.magic, "LBMXCKP2", 8);
     hd.nx = h->g.nx; hd.ny = h->g.ny; hd.pitch = h->g.pitch; hd.nplanes = h->nplanes;
     hd.storage = h->p.storage; hd.op = h->p.op; hd.periodic_x = h->g.periodic_x; hd.periodic_y = h->g.periodic_y;
     hd.quirks = h->p.quirks; hd.t = h->t;
@@ -909,7 +909,7 @@ lbmx_status lbmx_checkpoint_load(lbmx_handle* h, const char* path) {
     FILE* fp = fopen(path, "rb");
     if (!fp) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: cannot open %s", path);
     CheckpointHeader hd;
-    if (fread(&hd, sizeof(hd), 1, fp) != 1 || memcmp(hd.magic, "LBMXCKP1", 8) != 0) {
+    if (fread(&hd, sizeof(hd), 1, fp) != 1 || memcmp(hd.magic, "LBMXCKP2", 8) != 0) {
         fclose(fp);
         return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_checkpoint_load: %s is not an lbmx checkpoint", path);
     }

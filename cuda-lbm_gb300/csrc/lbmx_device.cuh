@@ -62,9 +62,10 @@ __device__ __forceinline__ float vpos_or(float a, float alt) { return a > 0.f ? 
 // ---------------------------------------------------------------- storage
 // FP32 stores f itself; the 16-bit forms store the offset f - w_q, which is
 // O(|u|) instead of O(1) and so keeps 10 (FP16) or 7 (BF16) significant bits
-// for the part of f that carries the flow.  FP16 holds the offset times
-// 2^12 (exact both ways), so offsets down to 2^-26 stay in FP16's normal
-// range instead of its coarse subnormals.
+// for the part of f that carries the flow.  Offsets below FP16's normal
+// range (2^-14) land on its subnormal grid of 2^-24; rounded stochastically
+// that costs noise of at most 6e-8 per store, far below the 2^-11-relative
+// noise of the offsets that carry the flow.
 //
 // Stores round stochastically by default: up with probability equal to the
 // discarded fraction of the gap to the next representable value (Forsythe
@@ -151,14 +152,13 @@ template <> struct Store<float> {
     static __device__ __forceinline__ void st2r_sr_u(float* p, float2 v, uint32_t) { p[0] = v.x; p[1] = v.y; }
 };
 template <> struct Store<__half> {
-    static constexpr float kUp = 4096.0f, kDown = 1.0f / 4096.0f;  // 2^12 storage scale
-    static __device__ __forceinline__ float ldr(const __half* p) { return __half2float(*p) * kDown; }
+    static __device__ __forceinline__ float ldr(const __half* p) { return __half2float(*p); }
     static __device__ __forceinline__ float2 ld2r(const __half* p) {
-        return __fmul2_rn(__half22float2(*reinterpret_cast<const __half2*>(p)), make_float2(kDown, kDown));
+        return __half22float2(*reinterpret_cast<const __half2*>(p));
     }
-    static __device__ __forceinline__ void str(__half* p, float v) { *p = __float2half_rn(v * kUp); }
+    static __device__ __forceinline__ void str(__half* p, float v) { *p = __float2half_rn(v); }
     static __device__ __forceinline__ void st2r(__half* p, float2 v) {
-        *reinterpret_cast<__half2*>(p) = __float22half2_rn(__fmul2_rn(v, make_float2(kUp, kUp)));
+        *reinterpret_cast<__half2*>(p) = __float22half2_rn(v);
     }
     static __device__ __forceinline__ float ld(const __half* p, float w) { return w + ldr(p); }
     static __device__ __forceinline__ void st(__half* p, float v, float w) { str(p, v - w); }
@@ -169,26 +169,24 @@ template <> struct Store<__half> {
     static __device__ __forceinline__ void st2(__half* p, float2 v, float w) { st2r(p, make_float2(v.x - w, v.y - w)); }
     // r16: 16 random bits (bits 15:0); r: a pair's 32
     static __device__ __forceinline__ void str_sr(__half* p, float v, uint32_t r16) {
-        *reinterpret_cast<unsigned short*>(p) = sr_half_bits(v * kUp, r16);
+        *reinterpret_cast<unsigned short*>(p) = sr_half_bits(v, r16);
     }
     static __device__ __forceinline__ void st2r_sr(__half* p, float2 v, uint32_t r) {
-        const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
-        *reinterpret_cast<uint32_t*>(p) = cvt_rs_f16x2(s.y, s.x, r);
+        *reinterpret_cast<uint32_t*>(p) = cvt_rs_f16x2(v.y, v.x, r);
     }
     static __device__ __forceinline__ void st_sr(__half* p, float v, float w, uint32_t r16) { str_sr(p, v - w, r16); }
     // two consecutive values at any (element-aligned) address: converted and
     // scaled as a pair, moved as two halves
     static __device__ __forceinline__ float2 ld2r_u(const __half* p) {
-        return __fmul2_rn(__half22float2(__halves2half2(p[0], p[1])), make_float2(kDown, kDown));
+        return __half22float2(__halves2half2(p[0], p[1]));
     }
     static __device__ __forceinline__ void st2r_u(__half* p, float2 v) {
-        const __half2 h = __float22half2_rn(__fmul2_rn(v, make_float2(kUp, kUp)));
+        const __half2 h = __float22half2_rn(v);
         p[0] = __low2half(h);
         p[1] = __high2half(h);
     }
     static __device__ __forceinline__ void st2r_sr_u(__half* p, float2 v, uint32_t r) {
-        const float2 s = __fmul2_rn(v, make_float2(kUp, kUp));
-        const uint32_t d = cvt_rs_f16x2(s.y, s.x, r);
+        const uint32_t d = cvt_rs_f16x2(v.y, v.x, r);
         reinterpret_cast<unsigned short*>(p)[0] = (unsigned short)(d & 0xFFFFu);
         reinterpret_cast<unsigned short*>(p)[1] = (unsigned short)(d >> 16);
     }
