@@ -15,7 +15,7 @@
 #include "lbmx_handle.h"
 
 namespace lbmx {
-size_t ibm_smem_bytes(int npatch, int nm);
+size_t ibm_smem_bytes(int npatch, int nm, int stencil);
 }
 
 using namespace lbmx;
@@ -525,9 +525,6 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
     if (h->has_aux_bc)
         LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_edge_prepass<decltype(tag)>(a, h->aux, st); }));
     if (h->nm > 0) {
-        LBMX_CUDA(h, dispatch(storage, [&](auto tag) {
-                      return launch_ibm_gather<decltype(tag)>(a, h->patch_nodes, h->npatch, h->patch_rho, h->patch_u, st);
-                  }));
         IbmArgs ia;
         ia.nm = h->nm;
         ia.npatch = h->npatch;
@@ -545,7 +542,9 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
         ia.plane = h->g.plane;
         ia.clamp = (h->p.quirks & LBMX_QUIRK_IBM_CLAMP) ? 1 : 0;
         ia.ds = h->p.ibm_ds;
-        LBMX_CUDA(h, launch_ibm_iterate(ia, st));
+        LBMX_CUDA(h, dispatch(storage, [&](auto tag) {
+                      return launch_ibm_step<decltype(tag)>(a, ia, h->patch_rho, h->patch_u, st);
+                  }));
     }
     const bool opt = h->p.op == LBMX_CM_OPT;
     const bool lagged = opt && (h->p.options & LBMX_OPTION_LAGGED_AVERAGES) && h->have_avg;
@@ -788,7 +787,7 @@ lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
     const int bad = lbmx::ibm_build_stencil(g.nx, g.ny, g.pitch, two, hxy.data(), n, sidx, sw, nodes);
     if (bad >= 0) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: marker %d is not finite", bad);
     const int np = (int)nodes.size();
-    if (lbmx::ibm_smem_bytes(np, n) > 200 * 1024)
+    if (lbmx::ibm_smem_bytes(np, n, S) > 200 * 1024)
         return fail(h, LBMX_ERR_TOO_LARGE, "lbmx_ibm_set_markers: %d markers touch %d nodes; limit is 200 KB of patch state",
                     n, np);
     h->nm = n;

@@ -110,10 +110,6 @@ template <typename T>
 cudaError_t launch_init(const StepArgs& a, const float* rho, const float* u, cudaStream_t s);
 template <typename T>
 cudaError_t launch_get_populations(const StepArgs& a, float* out, cudaStream_t s);
-template <typename T>
-cudaError_t launch_ibm_gather(const StepArgs& a, const int* patch_nodes, int npatch,
-                              float* patch_rho, float* patch_u, cudaStream_t s);
-
 // IBM multi-direct forcing on the marker patch (lbmx_ibm.cu)
 // The marker rounds' data; R is float for the engine and a tangent number
 // for the tangent-linear model.
@@ -134,7 +130,9 @@ struct IbmData {
     float ds;
 };
 using IbmArgs = IbmData<float>;
-cudaError_t launch_ibm_iterate(const IbmArgs& a, cudaStream_t s);
+// the IBM of one step: patch gather and marker rounds (lbmx_kernels.cuh)
+template <typename T>
+cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, float* patch_rho, float* patch_u, cudaStream_t s);
 
 // Many lattices in one persistent launch (lbmx_batch.cu).  Work items are
 // interior tiles and chunks of special units of every lattice; the

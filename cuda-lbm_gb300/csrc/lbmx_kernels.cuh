@@ -24,6 +24,7 @@
 #include <cstring>
 
 #include "lbmx_device.cuh"
+#include "lbmx_ibm.cuh"
 
 namespace lbmx {
 
@@ -727,29 +728,39 @@ __global__ void get_populations_kernel(const StepArgs a, float* out, int last_pa
     }
 }
 
-// Density and uncorrected velocity of the IBM patch nodes (the reference
-// interpolates from d_rho and the copy of d_u taken before the force
-// correction, IBMManager.cuh:227-228).
+// The IBM of one step in one CTA: density and uncorrected velocity of the
+// patch nodes (the reference interpolates from d_rho and the copy of d_u
+// taken before the force correction, IBMManager.cuh:227-228), then the
+// multi-direct rounds (ibm_rounds, lbmx_ibm.cuh).  Launched with programmatic
+// stream serialization like the step kernel: it waits for the previous step
+// before reading the populations and lets the next step kernel launch and
+// wait behind it.
 template <typename T>
-__global__ void ibm_gather_kernel(const StepArgs a, const int* patch_nodes, int npatch, float* prho, float* pu) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npatch) return;
-    const int off = patch_nodes[i];
-    const int y = off / a.g.pitch, x = off - y * a.g.pitch;
-    float f[9];
-    unsigned m;
-    gather_node<T>(a, x, y, f, &m);
-    float rho = 0.f, jx = 0.f, jy = 0.f;
+__global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a, const IbmArgs ib, float* prho,
+                                                               float* pu) {
+    extern __shared__ float sm[];
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" :::);
+    for (int i = threadIdx.x; i < ib.npatch; i += blockDim.x) {
+        const int off = ib.patch_nodes[i];
+        const int y = off / a.g.pitch, x = off - y * a.g.pitch;
+        float f[9];
+        unsigned m;
+        gather_node<T>(a, x, y, f, &m);
+        float rho = 0.f, jx = 0.f, jy = 0.f;
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-        rho += f[q];
-        jx += (float)CX(q) * f[q];
-        jy += (float)CY(q) * f[q];
+        for (int q = 0; q < 9; q++) {
+            rho += f[q];
+            jx += (float)CX(q) * f[q];
+            jy += (float)CY(q) * f[q];
+        }
+        const float inv = 1.0f / rho;
+        prho[i] = rho;
+        pu[i] = jx * inv;
+        pu[ib.npatch + i] = jy * inv;
     }
-    const float inv = 1.0f / rho;
-    prho[i] = rho;
-    pu[i] = jx * inv;
-    pu[npatch + i] = jy * inv;
+    __syncthreads();
+    ibm_rounds<float>(ib, reinterpret_cast<float*>(sm));
 }
 
 template <typename T, int OP, int P, int MODE>
@@ -834,11 +845,30 @@ cudaError_t launch_get_populations(const StepArgs& a, float* out, cudaStream_t s
 }
 
 template <typename T>
-cudaError_t launch_ibm_gather(const StepArgs& a, const int* patch_nodes, int npatch, float* prho, float* pu,
-                              cudaStream_t s) {
-    if (npatch <= 0) return cudaSuccess;
-    ibm_gather_kernel<T><<<(npatch + 127) / 128, 128, 0, s>>>(a, patch_nodes, npatch, prho, pu);
-    return cudaGetLastError();
+cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, float* prho, float* pu, cudaStream_t s) {
+    if (ib.npatch <= 0) return cudaSuccess;
+    const size_t smem = ibm_smem_bytes_of<float>(ib.npatch, ib.nm, ib.stencil);
+    // the attribute grows with the patch: raise it when a larger one comes
+    static int configured[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if ((int)smem > configured[dev & 63]) {
+        cudaError_t e = cudaFuncSetAttribute(ibm_step_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured[dev & 63] = (int)smem;
+    }
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(kIbmThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, ibm_step_kernel<T>, a, ib, prho, pu);
 }
 
 #define LBMX_INSTANTIATE(T)                                                                              \
@@ -847,6 +877,6 @@ cudaError_t launch_ibm_gather(const StepArgs& a, const int* patch_nodes, int npa
     template cudaError_t launch_edge_prepass<T>(const StepArgs&, float*, cudaStream_t);                  \
     template cudaError_t launch_init<T>(const StepArgs&, const float*, const float*, cudaStream_t);      \
     template cudaError_t launch_get_populations<T>(const StepArgs&, float*, cudaStream_t);               \
-    template cudaError_t launch_ibm_gather<T>(const StepArgs&, const int*, int, float*, float*, cudaStream_t);
+    template cudaError_t launch_ibm_step<T>(const StepArgs&, const IbmArgs&, float*, float*, cudaStream_t);
 
 }  // namespace lbmx

@@ -431,7 +431,7 @@ lbmx_status lbmx_tangent_set_markers(lbmx_tangent* t, const float* xy, int32_t n
     const int bad = ibm_build_stencil(t->p.nx, t->p.ny, t->p.nx, two, hxy.data(), n, sidx, sw, nodes);
     if (bad >= 0) return tfail(t, LBMX_ERR_INVALID_ARGUMENT, "lbmx_tangent_set_markers: marker %d is not finite", bad);
     const int np = (int)nodes.size();
-    if (ibm_smem_bytes_of<D>(np, n) > 200 * 1024)
+    if (ibm_smem_bytes_of<D>(np, n, two ? 2 : 4) > 200 * 1024)
         return tfail(t, LBMX_ERR_TOO_LARGE,
                      "lbmx_tangent_set_markers: %d markers touch %d nodes; limit is 200 KB of patch state", n, np);
     t->nm = n;
@@ -452,7 +452,7 @@ lbmx_status lbmx_tangent_set_markers(lbmx_tangent* t, const float* xy, int32_t n
     TAN_CUDA(t, cudaMemset(t->ibm_force, 0, 2 * (size_t)t->n * sizeof(D)));
     TAN_CUDA(t, cudaMemset(t->marker_force, 0, 2 * (size_t)n * sizeof(D)));
     TAN_CUDA(t, cudaFuncSetAttribute(tan_ibm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ibm_smem_bytes_of<D>(np, n)));
+                                     (int)ibm_smem_bytes_of<D>(np, n, t->stencil)));
     t->args.ibm_force = t->ibm_force;
     t->args.forced = 1;
     return LBMX_OK;
@@ -488,7 +488,7 @@ lbmx_status lbmx_tangent_run(lbmx_tangent* t, int32_t nsteps, double* series) {
     ia.plane = t->n;
     ia.clamp = (t->p.quirks & LBMX_QUIRK_IBM_CLAMP) ? 1 : 0;
     ia.ds = t->p.ibm_ds != 0.0f ? t->p.ibm_ds : 1.0f;
-    const size_t ibm_smem = ibm_smem_bytes_of<D>(t->npatch, t->nm);
+    const size_t ibm_smem = ibm_smem_bytes_of<D>(t->npatch, t->nm, t->stencil);
     for (int s = 0; s < nsteps; s++) {
         const float* pin = t->buf[t->cur];
         float* pout = t->buf[t->cur ^ 1];
