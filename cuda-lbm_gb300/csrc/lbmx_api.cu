@@ -339,7 +339,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     ALLOC(h->u_out, (size_t)2 * g.plane * sizeof(float));
     ALLOC(h->staging, (size_t)3 * n * sizeof(float));
     ALLOC(h->counter, sizeof(unsigned int));
-    ALLOC(h->sums, 6 * sizeof(double));
+    ALLOC(h->sums, kNumSums * sizeof(double));
     ALLOC(h->avg, 3 * sizeof(float));
     ALLOC(h->error_word, sizeof(unsigned int));
     ALLOC(h->tile_counter, 2 * sizeof(unsigned long long));
@@ -355,7 +355,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
         h->own_stream = true;
     }
     cudaMemsetAsync(h->counter, 0, sizeof(unsigned int), h->stream);
-    cudaMemsetAsync(h->sums, 0, 6 * sizeof(double), h->stream);
+    cudaMemsetAsync(h->sums, 0, kNumSums * sizeof(double), h->stream);
     cudaMemsetAsync(h->avg, 0, 3 * sizeof(float), h->stream);
     cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream);
     cudaMemsetAsync(h->tile_counter, 0, 2 * sizeof(unsigned long long), h->stream);
@@ -503,15 +503,17 @@ lbmx_status lbmx_init_from_fields(lbmx_handle* h, const float* rho, const float*
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
     h->t = 0;
     h->last_step = -2;
-    h->pend_acc = h->pend_series3 = nullptr;
+    h->pend_acc = h->pend_series = nullptr;
     h->initialized = true;
     h->have_avg = false;
     return LBMX_OK;
 }
 
 // One step (index s = t+1); store: write moments and FP64 sums; sums: the
-// FP64 sums only; series3: where the last block also writes sums 0..2.
-static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, double* series3 = nullptr) {
+// FP64 sums only; ke: the sums include the kinetic energy; series: where the
+// step's series entry (sums 0..2, then the kinetic energy) also goes.
+static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, bool ke,
+                            double* series = nullptr) {
     const long long s = h->t + 1;
     StepArgs a = base_args(h);
     set_step(h, a, s);
@@ -565,22 +567,23 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
         a.partials = acc;
         a.counter = h->counter;
         a.sums = (store || sums) ? h->sums : nullptr;
+        a.ke = (store || sums) && ke ? 1 : 0;
         // lagged CM_OPT: the averages of this step feed the next one
         a.avg_out = lagged ? h->avg : nullptr;
     }
     a.check_finite = check ? 1 : 0;
-    a.series3 = series3;
+    a.series = series;
     // the previous step's sums, if it left them to this launch
     if (h->pend_acc) {
         a.pub_acc = h->pend_acc;
         a.pub_sums = h->sums;
-        a.pub_series3 = h->pend_series3;
-        h->pend_acc = h->pend_series3 = nullptr;
+        a.pub_series = h->pend_series;
+        h->pend_acc = h->pend_series = nullptr;
     }
     LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_step<decltype(tag)>(a, h->tmap, h->p.op, st); }));
     if (step_mode(a) == kModeSums) {
         h->pend_acc = acc;
-        h->pend_series3 = series3;
+        h->pend_series = series;
     }
     h->last_step = s;
     h->t = s;
@@ -590,8 +593,8 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, d
 // Publish sums a step left to the next launch when no step follows.
 static lbmx_status flush_sums(lbmx_handle* h) {
     if (!h->pend_acc) return LBMX_OK;
-    LBMX_CUDA(h, launch_publish(h->pend_acc, h->sums, h->pend_series3, h->stream));
-    h->pend_acc = h->pend_series3 = nullptr;
+    LBMX_CUDA(h, launch_publish(h->pend_acc, h->sums, h->pend_series, h->stream));
+    h->pend_acc = h->pend_series = nullptr;
     return LBMX_OK;
 }
 
@@ -602,10 +605,11 @@ lbmx_status lbmx_step_ex(lbmx_handle* h, int32_t nsteps, uint32_t flags) {
     cudaSetDevice(h->p.device);
     const bool check = (flags & LBMX_STEP_CHECK_FINITE) != 0;
     if (check) LBMX_CUDA(h, cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream));
+    const bool ke = (flags & LBMX_STEP_KINETIC_ENERGY) != 0;
     for (int i = 0; i < nsteps; i++) {
         const bool last = i == nsteps - 1;
-        lbmx_status st =
-            run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, (flags & LBMX_STEP_SUMS) != 0);
+        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check,
+                                  (flags & LBMX_STEP_SUMS) != 0, ke);
         if (st != LBMX_OK) return st;
     }
     lbmx_status fs = flush_sums(h);
@@ -637,15 +641,21 @@ lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, doubl
     else
         cudaGetLastError();
     double* dev_series = direct ? static_cast<double*>(attr.devicePointer) : nullptr;
+    // a step's entry: {rho, rho ux, rho uy}, then the kinetic energy
+    const bool ke = (flags & LBMX_STEP_KINETIC_ENERGY) != 0;
+    const size_t stride = ke ? 4 : 3;
     for (int i = 0; i < nsteps; i++) {
         const bool last = i == nsteps - 1;
-        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, true,
-                                  direct ? dev_series + 3 * (size_t)i : nullptr);
+        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check, true, ke,
+                                  direct ? dev_series + stride * (size_t)i : nullptr);
         if (st != LBMX_OK) return st;
         if (!direct) {
             if ((st = flush_sums(h)) != LBMX_OK) return st;
-            LBMX_CUDA(h, cudaMemcpyAsync(series + 3 * (size_t)i, h->sums, 3 * sizeof(double), cudaMemcpyDefault,
-                                         h->stream));
+            LBMX_CUDA(h, cudaMemcpyAsync(series + stride * (size_t)i, h->sums, 3 * sizeof(double),
+                                         cudaMemcpyDefault, h->stream));
+            if (ke)
+                LBMX_CUDA(h, cudaMemcpyAsync(series + stride * (size_t)i + 3, h->sums + kSumKE, sizeof(double),
+                                             cudaMemcpyDefault, h->stream));
         }
     }
     lbmx_status fs = flush_sums(h);
@@ -668,6 +678,17 @@ lbmx_status lbmx_moment_sums_async(lbmx_handle* h, double* sums3) {
     if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_moment_sums_async: not initialized");
     cudaSetDevice(h->p.device);
     LBMX_CUDA(h, cudaMemcpyAsync(sums3, h->sums, 3 * sizeof(double), cudaMemcpyDefault, h->stream));
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_kinetic_energy(lbmx_handle* h, double* ke) {
+    if (!h || !ke) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_kinetic_energy: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_kinetic_energy: not initialized");
+    cudaSetDevice(h->p.device);
+    double v = 0.0;
+    LBMX_CUDA(h, cudaMemcpyAsync(&v, h->sums + kSumKE, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    *ke = v;
     return LBMX_OK;
 }
 
@@ -940,7 +961,7 @@ lbmx_status lbmx_checkpoint_load(lbmx_handle* h, const char* path) {
     LBMX_CUDA(h, cudaMemcpy(h->avg, avg, sizeof(avg), cudaMemcpyHostToDevice));
     h->t = hd.t;
     h->last_step = -2;
-    h->pend_acc = h->pend_series3 = nullptr;
+    h->pend_acc = h->pend_series = nullptr;
     h->initialized = true;
     h->have_avg = h->p.op == LBMX_CM_OPT && hd.t > 0;
     return LBMX_OK;

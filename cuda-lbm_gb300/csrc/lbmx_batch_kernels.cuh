@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
             for (int j = max(0, k - St::NST); j < k; j++)
                 mbar_wait(&full[j % St::NST], (unsigned)((j / St::NST) & 1), kWaitLimit);
     } else {
-        Acc v[6] = {0, 0, 0, 0, 0, 0};  // unused: batched steps keep no grid sums
+        Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};  // unused: batched steps keep no grid sums
         const int lx = tid % (TW / 2), r0 = tid / (TW / 2);
         for (int i = 0;; i++) {
             const int s = i % St::NST;

@@ -61,7 +61,7 @@ struct lbmx_handle {
     unsigned long long* tile_counter = nullptr;  // [2] work counters, alternating by step
     long long last_step = -2;      // step index of the last single-lattice launch
     double* pend_acc = nullptr;    // accumulators of a step whose sums are not yet published
-    double* pend_series3 = nullptr;
+    double* pend_series = nullptr; // and that step's series entry or null
     int tile_chunk = 1;
     CUtensorMap tmap;  // the type carries the 64-byte alignment TMA needs  // TMA descriptor of the population planes
     long long partial_cap = 0;

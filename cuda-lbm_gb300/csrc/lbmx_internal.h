@@ -38,10 +38,12 @@ struct StepArgs {
     const float* avg;        // CM_OPT grid averages {rho, |j|, |Pi|} (device)
     float* rho_out;          // [plane] moments written when non-null
     float* u_out;            // [2][plane]
-    double* partials;        // [blocks][6] FP64 block sums when non-null
+    double* partials;        // one accumulator set of the grid sums (kAccPerSet) when non-null
     unsigned int* counter;   // last-block-done counter for the sums
-    double* sums;            // [6] final sums
-    double* series3;         // or null: the last block also writes sums 0..2 here (device-accessible)
+    double* sums;            // [kNumSums] final sums
+    double* series;          // or null: the sums' series entry (sums 0..2, then the kinetic
+                             // energy when `ke`) is also written here (device-accessible)
+    int ke;                  // the sums include the kinetic energy 1/2 rho |u|^2 (accumulator kSumKE)
     float* avg_out;          // averages produced by the last block (lagged CM_OPT / pre-pass)
     unsigned int* error_word;// bit 0: non-finite density seen, bit 1: a staging wait gave up
     int check_finite;        // look for non-finite densities this step
@@ -77,10 +79,10 @@ struct StepArgs {
     int tile_chunk;                    // consecutive tiles taken per claim
     // sums of the previous step left for this launch to publish (kModeSums
     // steps publish one launch late; see step_mode): accumulators, the
-    // six-entry sums array, the series entry or null
+    // sums array, the series entry or null
     double* pub_acc;
     double* pub_sums;
-    double* pub_series3;
+    double* pub_series;
 };
 
 // Seed of the stochastic-rounding hash for step index s (a Weyl sequence:
@@ -159,11 +161,16 @@ cudaError_t launch_batch_step(const BatchArgs& b, int op, int parity, int tile_w
 // kernel also runs 64 x 8 and 128 x 8 tiles.
 constexpr int kStepThreads = 288;  // 8 consumer warps + 1 producer warp
 constexpr int kConsumerWarps = 8;
-// Grid sums go into kSumSlots copies of the six fixed-point accumulators
-// (warp w of CTA b adds to slot (9 b + w) % kSumSlots), so few warps contend
-// for one address; a handle holds two such sets, one per step parity.
+// The grid sums of a step: 0-2 mass and momentum {rho, rho ux, rho uy},
+// 3 the kinetic energy 1/2 rho |u|^2, 4-5 the CM_OPT average terms
+// {rho |u|, |Pi|} (their third, <rho>, is sum 0 over the node count).  They
+// go into kSumSlots copies of the kNumSums fixed-point accumulators (warp w
+// of CTA b adds to slot (9 b + w) % kSumSlots), so few warps contend for one
+// address; a handle holds two such sets, one per step parity.
+constexpr int kNumSums = 6;
+constexpr int kSumKE = 3;
 constexpr int kSumSlots = 32;
-constexpr int kAccPerSet = kSumSlots * 6;
+constexpr int kAccPerSet = kSumSlots * kNumSums;
 
 // Interior-path variant of a step launch:
 //   kModeLean  no per-node force or Brinkman field, no moment store, no sums,
@@ -171,17 +178,20 @@ constexpr int kAccPerSet = kSumSlots * 6;
 //   kModeSums  the lean path plus the mass / momentum sums, published by the
 //              next launch on the stream (or lbmx's publish kernel), so the
 //              step itself ends with no fence or counter;
-//   kModeFull  everything, decided per launch from the arguments; the last
-//              CTA publishes its own sums.
+//   kModeFull  everything, decided per launch from the arguments (the
+//              kinetic energy among them: one more live accumulator would
+//              cost the kModeSums variants registers); the last CTA
+//              publishes its own sums.
 constexpr int kModeLean = 0, kModeSums = 1, kModeFull = 2;
 inline int step_mode(const StepArgs& a) {
     const bool plain = !a.force && !a.gamma && !a.rho_out && !a.check_finite;
     if (plain && !a.partials) return kModeLean;
-    if (plain && !a.avg_out) return kModeSums;
+    if (plain && !a.avg_out && !a.ke) return kModeSums;
     return kModeFull;
 }
-// publishes the sums in acc (one accumulator set) into sums / series3
-cudaError_t launch_publish(double* acc, double* sums, double* series3, cudaStream_t s);
+// publishes the mass and momentum sums in acc (one accumulator set) into
+// sums / series
+cudaError_t launch_publish(double* acc, double* sums, double* series, cudaStream_t s);
 constexpr int kCtasPerSm = 3;      // resident persistent CTAs per SM (72 registers per thread)
 constexpr int kStageW = 128;
 constexpr int kStageH = 4;

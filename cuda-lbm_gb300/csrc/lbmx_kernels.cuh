@@ -30,30 +30,39 @@ namespace lbmx {
 
 constexpr int kThreads = kStepThreads;
 
-// The step's grid sums (mass, momentum and the CM_OPT average terms) are
-// accumulated in exact 64-bit fixed point: each node's FP32 term, scaled by
-// 2^30 and rounded, is added as an integer -- per thread, by warp shuffles,
-// then across warps with integer atomics into six accumulators
-// (partials[0..5]).  Integer addition is associative, so the sums are the
-// same bit for bit whichever CTA claims which tile; a term's rounding is at
-// most 2^-31 (5e-10), and the range (|sum| < 2^33) covers any lattice of up
-// to 2^31 nodes at unit density.  The reference adds float atomics
-// (update_avg_mag, macroscopics.cuh:116-118); FP64 arithmetic, a small
-// fraction of FP32's rate on GB300, appears only in the final conversion.
+// The step's grid sums (mass, momentum, the CM_OPT average terms and the
+// kinetic energy; kNumSums of them) are accumulated in exact 64-bit fixed
+// point: each node's FP32 term, scaled by 2^30 and rounded, is added as an
+// integer -- per thread, by warp shuffles, then across warps with integer
+// atomics into the accumulators of a slot.  Integer addition is
+// associative, so the sums are the same bit for bit whichever CTA claims
+// which tile; a term's rounding is at most 2^-31 (5e-10), and the range
+// (|sum| < 2^33) covers any lattice of up to 2^31 nodes at unit density.
+// The reference adds float atomics (update_avg_mag,
+// macroscopics.cuh:116-118; compute_kinetic_energy_kernel,
+// scenarios/taylorGreen3D/postprocessing/kineticEnergy.cuh:7-40); FP64
+// arithmetic, a small fraction of FP32's rate on GB300, appears only in the
+// final conversion.
 using Acc = long long;
 constexpr float kFixScale = 1073741824.0f;  // 2^30
 __device__ __forceinline__ Acc fix(float t) { return __float2ll_rn(t * kFixScale); }
 
-// A warp's totals of the first nsum accumulators into its slot.
-__device__ __forceinline__ void warp_sums(double* partials, const Acc v[6], int nsum) {
+// which accumulators a set of sums uses: mass and momentum always, the
+// kinetic energy and the CM_OPT average terms on request
+__host__ __device__ __forceinline__ unsigned sums_mask(bool ke, bool averages) {
+    return 0x7u | (ke ? 1u << kSumKE : 0u) | (averages ? 0x30u : 0u);
+}
+
+// A warp's totals of the accumulators in `mask` into its slot.
+__device__ __forceinline__ void warp_sums(double* partials, const Acc v[kNumSums], unsigned mask) {
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const int nwarps = (blockDim.x * blockDim.y + 31) >> 5;
     unsigned long long* acc =
-        reinterpret_cast<unsigned long long*>(partials) + ((blockIdx.x * nwarps + warp) % kSumSlots) * 6;
+        reinterpret_cast<unsigned long long*>(partials) + ((blockIdx.x * nwarps + warp) % kSumSlots) * kNumSums;
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-        if (k >= nsum) break;
+    for (int k = 0; k < kNumSums; k++) {
+        if (!((mask >> k) & 1u)) continue;
         Acc t = v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
@@ -61,38 +70,47 @@ __device__ __forceinline__ void warp_sums(double* partials, const Acc v[6], int 
     }
 }
 
-// The first nsum sums of an accumulator set (integer sums over the slots:
-// the same bits in any order), zeroing the set for its next use.
-__device__ __forceinline__ void collect_sums(double* partials, int nsum, double s[6]) {
+// The sums in `mask` of an accumulator set (integer sums over the slots: the
+// same bits in any order), zeroing them for their next use; the others are 0.
+__device__ __forceinline__ void collect_sums(double* partials, unsigned mask, double s[kNumSums]) {
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials);
-    for (int k = 0; k < 6; k++) s[k] = 0.0;
-    for (int k = 0; k < nsum; k++) {
+    for (int k = 0; k < kNumSums; k++) {
+        s[k] = 0.0;
+        if (!((mask >> k) & 1u)) continue;
         unsigned long long t = 0;
         for (int j = 0; j < kSumSlots; j++) {
-            t += __ldcg(acc + j * 6 + k);
-            acc[j * 6 + k] = 0ull;
+            t += __ldcg(acc + j * kNumSums + k);
+            acc[j * kNumSums + k] = 0ull;
         }
         s[k] = (double)(long long)t * (1.0 / (double)kFixScale);
     }
 }
 
-// Publish a kModeSums step's sums (one thread).
-__device__ __forceinline__ void publish_sums(double* partials, double* sums, double* series3) {
-    double s[6];
-    collect_sums(partials, 3, s);
+// The sums array and a step's series entry: {rho, rho ux, rho uy}, then the
+// kinetic energy when it was reduced.
+__device__ __forceinline__ void write_sums(const double s[kNumSums], double* sums, double* series, bool ke) {
     if (sums)
-        for (int k = 0; k < 6; k++) sums[k] = s[k];
-    if (series3)
-        for (int k = 0; k < 3; k++) series3[k] = s[k];
+        for (int k = 0; k < kNumSums; k++) sums[k] = s[k];
+    if (series) {
+        for (int k = 0; k < 3; k++) series[k] = s[k];
+        if (ke) series[3] = s[kSumKE];
+    }
+}
+
+// Publish a kModeSums step's sums (one thread): mass and momentum only.
+__device__ __forceinline__ void publish_sums(double* partials, double* sums, double* series) {
+    double s[kNumSums];
+    collect_sums(partials, sums_mask(false, false), s);
+    write_sums(s, sums, series, false);
 }
 
 // Grid reduction of the accumulators; the last CTA to finish publishes the
 // sums (sums, series, averages) and zeroes the accumulators for the next launch.
-__device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], long long n_nodes) {
+__device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[kNumSums], long long n_nodes) {
     __shared__ bool is_last;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nsum = a.avg_out ? 6 : 3;
-    warp_sums(a.partials, v, nsum);
+    const unsigned mask = sums_mask(a.ke != 0, a.avg_out != nullptr);
+    warp_sums(a.partials, v, mask);
     __syncthreads();
     if (tid == 0) {
         __threadfence();
@@ -102,14 +120,11 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[6], lo
     __syncthreads();
     if (!is_last || tid != 0) return;
     __threadfence();
-    double s[6];
-    collect_sums(a.partials, nsum, s);
-    if (a.sums)
-        for (int k = 0; k < 6; k++) a.sums[k] = s[k];
-    if (a.series3)
-        for (int k = 0; k < 3; k++) a.series3[k] = s[k];
+    double s[kNumSums];
+    collect_sums(a.partials, mask, s);
+    write_sums(s, a.sums, a.series, a.ke != 0);
     if (a.avg_out) {
-        a.avg_out[0] = (float)(s[3] / (double)n_nodes);
+        a.avg_out[0] = (float)(s[0] / (double)n_nodes);
         a.avg_out[1] = (float)(s[4] / (double)n_nodes);
         a.avg_out[2] = (float)(s[5] / (double)n_nodes);
     }
@@ -145,7 +160,7 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
 // code for boundary nodes, so a lattice gets bit-identical results from both
 // (inlined, the two callers may contract multiply-adds differently).
 template <typename T, int OP>
-__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[6], uint32_t seed) {
+__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[kNumSums], uint32_t seed) {
     const long long off = (long long)y * a.g.pitch + x;
     float f[9];
     unsigned outmask;
@@ -183,8 +198,8 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v
         v[0] += fix(rho);
         v[1] += fix(rho * ux);
         v[2] += fix(rho * uy);
+        if (a.ke) v[kSumKE] += fix(0.5f * rho * (ux * ux + uy * uy));
         if (a.avg_out) {
-            v[3] += fix(rho);
             v[4] += fix(rho * sqrtf(ux * ux + uy * uy));
             v[5] += fix(pimag);
         }
@@ -319,7 +334,7 @@ __host__ __device__ constexpr int mode_sums(int mode) { return mode == kModeLean
 // Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
 template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, int MODE = kModeFull>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
-                                              Acc v[6], uint32_t seed) {
+                                              Acc v[kNumSums], uint32_t seed) {
     using St = Staging<T, TW, TH>;
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
@@ -371,8 +386,11 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
         v[0] += fix(rho.v.x + rho.v.y);
         v[1] += fix(jx2.v.x + jx2.v.y);
         v[2] += fix(jy2.v.x + jy2.v.y);
+        if (MODE == kModeFull && a.ke) {
+            const V2 e2 = rho * fma(ux, ux, uy * uy);
+            v[kSumKE] += fix(0.5f * (e2.v.x + e2.v.y));
+        }
         if (MODE == kModeFull && a.avg_out) {
-            v[3] += fix(rho.v.x) + fix(rho.v.y);
             v[4] += fix(rho.v.x * sqrtf(ux.v.x * ux.v.x + uy.v.x * uy.v.x)) +
                     fix(rho.v.y * sqrtf(ux.v.y * ux.v.y + uy.v.y * uy.v.y));
             v[5] += fix(pimag.v.x) + fix(pimag.v.y);
@@ -415,7 +433,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
 // One chunk of special nodes: consumer thread t takes node `first + t` of
 // the special-unit list (two nodes per unit).
 template <typename T, int OP, int MODE = kModeFull>
-__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, Acc v[6], uint32_t seed) {
+__device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int tid, Acc v[kNumSums], uint32_t seed) {
     const int k = chunk * kSpecialChunk + tid;
     if (k >= 2 * a.nspecial) return;
     const int off = a.special_units[k >> 1];
@@ -423,7 +441,7 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
     if (x >= a.g.nx) return;
     // the out-of-line call gets its own accumulators, so the caller's stay
     // in registers
-    Acc t[6] = {0, 0, 0, 0, 0, 0};
+    Acc t[kNumSums] = {0, 0, 0, 0, 0, 0};
     general_node<T, OP>(a, x, y, t, seed);
     if (mode_sums(MODE) > 0 && a.partials)
 #pragma unroll
@@ -442,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     // landed (or at once for a special chunk); empty[s] when all eight
     // consumer warps are done with it.
     using St = Staging<T, TW, TH>;
-    Acc v[6] = {0, 0, 0, 0, 0, 0};
+    Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};
     const int tid = threadIdx.x;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* bufs = reinterpret_cast<T*>(smem_raw);
@@ -471,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
         // the next step's work counter (the previous launch used it and has
         // finished), and the previous step's sums if it left them
         *a.tile_counter_next = 0ull;
-        if (a.pub_acc) publish_sums(a.pub_acc, a.pub_sums, a.pub_series3);
+        if (a.pub_acc) publish_sums(a.pub_acc, a.pub_sums, a.pub_series);
     }
     __syncthreads();
     if (warp == kConsumerWarps) {
@@ -563,7 +581,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     }
     // kModeSums: each warp adds its totals and is done (the next launch
     // publishes them); kModeFull: the last CTA publishes
-    if (MODE == kModeSums) warp_sums(a.partials, v, 3);
+    if (MODE == kModeSums) warp_sums(a.partials, v, sums_mask(false, false));
     else if (MODE == kModeFull && a.partials) block_sums(a, v, (long long)a.g.nx * a.g.ny);
 }
 
@@ -572,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
 // collision (update_avg_mag, macroscopics.cuh:50-120), for CM_OPT.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a) {
-    Acc v[6] = {0, 0, 0, 0, 0, 0};
+    Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};
     const long long n = (long long)a.g.nx * a.g.ny;
     for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
         const int y = (int)(i / a.g.nx), xx = (int)(i - (long long)y * a.g.nx);
@@ -597,7 +615,7 @@ __global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a)
             const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
             const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
             const float pxy = f[5] - f[6] + f[7] - f[8];
-            v[3] += fix(rho);
+            v[0] += fix(rho);
             v[4] += fix(rho * sqrtf(ux * ux + uy * uy));
             v[5] += fix(sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy));
         }

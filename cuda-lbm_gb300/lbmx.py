@@ -25,13 +25,13 @@ QUIRK_REST_LAG, QUIRK_ZOUHE_LEFT, QUIRK_MRT_FORCE, QUIRK_IBM_2X2, QUIRK_IBM_CLAM
 QUIRKS_REFERENCE = 0x1F
 OPTION_LAGGED_AVERAGES = 1
 OPTION_ROUND_NEAREST = 2
-STEP_STORE_MOMENTS, STEP_CHECK_FINITE, STEP_SUMS = 1, 2, 4
+STEP_STORE_MOMENTS, STEP_CHECK_FINITE, STEP_SUMS, STEP_KINETIC_ENERGY = 1, 2, 4, 8
 
 STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INVALID_FLAGS",
           5: "NOT_INITIALIZED", 6: "UNSUPPORTED", 7: "NONFINITE", 8: "TOO_LARGE"}
 
 EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
-            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_moment_sums_async", "lbmx_step_sums",
+            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_moment_sums_async", "lbmx_step_sums", "lbmx_kinetic_energy",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
             "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc", "lbmx_checkpoint_save",
             "lbmx_checkpoint_load", "lbmx_write_vti", "lbmx_batch_create", "lbmx_batch_destroy",
@@ -97,6 +97,8 @@ def load_library(path=LIB_PATH):
     lib.lbmx_moment_sums_async.restype = ctypes.c_int32
     lib.lbmx_step_sums.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
     lib.lbmx_step_sums.restype = ctypes.c_int32
+    lib.lbmx_kinetic_energy.argtypes = [vp, vp]
+    lib.lbmx_kinetic_energy.restype = ctypes.c_int32
     lib.lbmx_get_populations.argtypes = [vp, vp]
     lib.lbmx_averages.argtypes = [vp, fp]
     lib.lbmx_ibm_set_markers.argtypes = [vp, vp, ctypes.c_int32]
@@ -240,6 +242,22 @@ class Lattice:
 
     def step(self, n=1, flags=STEP_STORE_MOMENTS):
         self._check(self.lib.lbmx_step_ex(self.h, int(n), int(flags)))
+
+    def step_sums(self, n, flags=0):
+        """n steps that reduce the FP64 sums of every step: an [n, 3] array of
+        {rho, rho ux, rho uy}, [n, 4] with the kinetic energy when flags has
+        STEP_KINETIC_ENERGY (lbmx_step_sums into pageable host memory)."""
+        width = 4 if flags & STEP_KINETIC_ENERGY else 3
+        out = np.zeros((int(n), width), np.float64)
+        self._check(self.lib.lbmx_step_sums(self.h, int(n), int(flags), out.ctypes.data))
+        self.synchronize()
+        return out
+
+    def kinetic_energy(self):
+        """1/2 sum rho |u|^2 of the last step that reduced it (lbmx_kinetic_energy)."""
+        v = ctypes.c_double()
+        self._check(self.lib.lbmx_kinetic_energy(self.h, ctypes.byref(v)))
+        return v.value
 
     def moments(self, rho=None, u=None):
         """(rho[ny,nx], u[2,ny,nx], sums[3]) of the last stored step, as numpy."""

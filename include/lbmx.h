@@ -90,7 +90,8 @@ enum {
 enum {
     LBMX_STEP_STORE_MOMENTS = 1u << 0, /* last step stores rho, u and the FP64 sums */
     LBMX_STEP_CHECK_FINITE = 1u << 1,  /* last step flags non-finite densities */
-    LBMX_STEP_SUMS = 1u << 2           /* every step reduces the FP64 sums (no fields stored) */
+    LBMX_STEP_SUMS = 1u << 2,          /* every step reduces the FP64 sums (no fields stored) */
+    LBMX_STEP_KINETIC_ENERGY = 1u << 3 /* the steps that reduce the sums also reduce the kinetic energy */
 };
 
 /* Replaces the compile-time NX/NY/PERIODIC_* macros and the Scenario
@@ -175,8 +176,21 @@ lbmx_status lbmx_moment_sums_async(lbmx_handle* h, double* sums3);
 /* nsteps steps (flags as lbmx_step_ex) that also reduce the FP64 sums of
  * every step into series[3 * k .. 3 * k + 2] for step k (pinned host or
  * device memory), copied without waiting; the series is complete once the
- * stream has reached the end (lbmx_synchronize). */
+ * stream has reached the end (lbmx_synchronize).  With
+ * LBMX_STEP_KINETIC_ENERGY a step's entry is four wide,
+ * series[4 * k .. 4 * k + 3] = {rho, rho*ux, rho*uy, kinetic energy}. */
 lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, double* series);
+
+/* The kinetic energy 1/2 sum rho |u|^2 (force-corrected u, the velocity
+ * lbmx_moments returns) of the last step that reduced the FP64 sums with
+ * LBMX_STEP_KINETIC_ENERGY set; 0 when that step's flags did not include it.
+ * Blocks until the stream has reached that step.  Replaces the reference's
+ * separate reduction pass over the stored fields, calculate_kinetic_energy /
+ * compute_kinetic_energy_kernel
+ * (src/scenarios/taylorGreen3D/postprocessing/kineticEnergy.cuh:7-40, there
+ * in 3-D with FP32 atomics); here it is fused into the step kernel in exact
+ * 64-bit fixed point, so it is the same bit for bit on every run. */
+lbmx_status lbmx_kinetic_energy(lbmx_handle* h, double* ke);
 
 /* Post-collision populations of the last step, out[9*n], population planes
  * in the reference's velocity order.  Slots whose value streamed out of a

@@ -161,3 +161,71 @@ def test_sums_match_the_stored_moments(storage, nx):
         assert abs(s[0] - r64.sum()) <= 2e-7 * r64.sum()
         assert abs(s[1] - (r64 * u[0]).sum()) <= 1e-6 * np.abs(r64 * u[0]).sum()
         assert abs(s[2] - (r64 * u[1]).sum()) <= 1e-6 * np.abs(r64 * u[1]).sum()
+
+
+def kinetic_energy_of(rho, u):
+    r64, u64 = rho.astype(np.float64), u.astype(np.float64)
+    return 0.5 * (r64 * (u64[0] ** 2 + u64[1] ** 2)).sum()
+
+
+@pytest.mark.parametrize("storage", [0, 1])
+@pytest.mark.parametrize("nx", [96, 99])
+def test_kinetic_energy_matches_the_stored_moments(storage, nx):
+    # LBMX_STEP_KINETIC_ENERGY: 1/2 sum rho |u|^2 reduced inside the step, in
+    # both step parities, on widths short of a whole tile
+    c = C.random_state(C.cavity_moving_wall(nx, 70, op=C.MRT), seed=11)
+    L = C.make_lattice(c, storage=storage)
+    for n in (3, 1):
+        L.step(n, flags=lbmx.STEP_STORE_MOMENTS | lbmx.STEP_KINETIC_ENERGY)
+        rho, u, _ = L.moments()
+        ref = kinetic_energy_of(rho, u)
+        ke = L.kinetic_energy()
+        # fixed-point terms of 2^-30; interior units add their two nodes' terms
+        # in FP32 first
+        assert abs(ke - ref) <= 1e-6 * ref + rho.size * 1e-9, (ke, ref)
+    # a step that reduces the sums without the flag reports no kinetic energy
+    L.step(1)
+    assert L.kinetic_energy() == 0.0
+
+
+def test_kinetic_energy_series():
+    # the four-wide series: mass and momentum bit for bit as without the
+    # flag, the kinetic energy bit for bit as single steps that store it;
+    # into pageable host memory (a copy per step) and device memory (written
+    # by the step kernel itself)
+    import torch
+    c = C.random_state(C.cavity_moving_wall(96, 72, op=C.MRT), seed=12)
+    n = 6
+    plain = C.make_lattice(c).step_sums(n)
+    host = C.make_lattice(c).step_sums(n, lbmx.STEP_KINETIC_ENERGY)
+    d = C.make_lattice(c)
+    dev = torch.zeros(4 * n, dtype=torch.float64, device="cuda")
+    d._check(d.lib.lbmx_step_sums(d.h, n, lbmx.STEP_KINETIC_ENERGY, dev.data_ptr()))
+    d.synchronize()
+    dev = dev.cpu().numpy().reshape(n, 4)
+    r = C.make_lattice(c)
+    single = []
+    for _ in range(n):
+        r.step(1, flags=lbmx.STEP_STORE_MOMENTS | lbmx.STEP_KINETIC_ENERGY)
+        single.append(r.kinetic_energy())
+    assert host.shape == (n, 4) and plain.shape == (n, 3)
+    np.testing.assert_array_equal(host[:, :3], plain)
+    np.testing.assert_array_equal(dev, host)
+    np.testing.assert_array_equal(host[:, 3], np.array(single))
+    assert np.all(host[:, 3] > 0)
+
+
+def test_kinetic_energy_decays_at_the_taylor_green_rate():
+    # u ~ exp(-nu (kx^2 + ky^2) t), so the kinetic energy decays at twice that
+    # rate; BGK on 64 x 64 nodes (k dx = 0.098) is within a fraction of a percent
+    c = C.taylor_green(64, 64, op=C.BGK, nu=0.01, u0=0.04)
+    L = C.make_lattice(c)
+    s = L.step_sums(600, lbmx.STEP_KINETIC_ENERGY)
+    ke = s[:, 3]
+    k2 = 2 * (2 * np.pi / 64) ** 2
+    rate = -np.log(ke[599] / ke[99]) / 500.0
+    assert abs(rate / (2 * 0.01 * k2) - 1.0) < 2e-2, rate / (2 * 0.01 * k2)
+    # the mass moves only by the FP32 rounding of the populations: about
+    # 1.4e-8 per node per step, 8e-6 of the mass in 600 steps, as much as a
+    # plain float32 numpy BGK step drifts on this case (float64: 1e-16)
+    assert np.all(np.abs(s[:, 0] - 64 * 64) <= 5e-5 * 64 * 64)
