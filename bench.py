@@ -57,7 +57,10 @@ for _p in (os.path.join(REPO, "cuda-lbm_gb300"), os.path.join(REPO, "oracle"), o
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = "MLUPS (D2Q9 lid-driven cavity 1024x1024 MRT, FP32 storage)"
+def metric_name(n, storage=0):
+    """The metric of a lid-driven cavity run on n x n nodes (the default run:
+    1024 x 1024, FP32 storage)."""
+    return "MLUPS (D2Q9 lid-driven cavity %dx%d MRT, %s storage)" % (n, n, ("FP32", "FP16-offset", "BF16-offset")[storage])
 BYTES_PER_LU = {0: 72, 1: 36, 2: 36}
 STORAGE_NAME = {0: "f32", 1: "f16_offset", 2: "bf16_offset"}
 
@@ -586,7 +589,7 @@ def bench_reference(args, rank, world):
     t = float(np.mean(times))
     mlups = n * n * per_step / t / 1e6
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
+        "impl": "reference", "metric": metric_name(n), "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3 / per_step, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "lid-driven cavity %dx%d MRT, lid 0.1, Re 1000" % (n, n), "nodes": n * n,
@@ -672,7 +675,7 @@ def main():
     mlups = aggregate_mlups(nodes, ms, world)
     achieved = BYTES_PER_LU[main_storage] * nodes / (float(t.mean()) * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "metric": metric_name(n, main_storage), "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "lid-driven cavity %dx%d, D2Q9 MRT, lid 0.1 half-way moving wall, Re 1000" % (n, n),
