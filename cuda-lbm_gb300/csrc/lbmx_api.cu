@@ -391,7 +391,7 @@ lbmx_status lbmx_set_flags(lbmx_handle* h, const uint8_t* flags) {
             if (fl == LBMX_ZOU_HE_TOP_LEFT_TOP_INFLOW || fl == LBMX_ZOU_HE_TOP_RIGHT_TOP_INFLOW)
                 return fail(h, LBMX_ERR_INVALID_FLAGS,
                             "lbmx_set_flags: flag %d at (%d,%d) is not implemented by the reference (it asserts)", fl, x, y);
-            if (fl > LBMX_HALFWAY_BB)
+            if (fl > LBMX_CORNER_BOTTOM_LEFT)
                 return fail(h, LBMX_ERR_INVALID_FLAGS, "lbmx_set_flags: unknown flag %d at (%d,%d)", fl, x, y);
             if (fl == LBMX_PRESSURE_OUTLET && (!edge || x == 0))
                 return fail(h, LBMX_ERR_INVALID_FLAGS,

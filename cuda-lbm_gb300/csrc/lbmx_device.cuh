@@ -511,6 +511,30 @@ __device__ __forceinline__ R parabolic_ux(R u_bc, int y, int ny) {
     return 4.0f * u_bc * (float)y * (h - (float)y) / (h * h);
 }
 
+// CornerBoundary (cornerBoundaries.cuh:38-82): Zou-He-style corners of a
+// left inlet whose velocity the reference fixes at ux = 0.03, uy = 0.  The
+// top-left one sets f2 from f4 and the bottom-left one f4 from f2, as the
+// reference does.  The reference's 2-D boundary kernel never dispatches them
+// (no BC_flag selects them); here they have flags of their own.
+template <typename R>
+__device__ __forceinline__ void bc_corner_top_left(R f[9]) {
+    const float ux = 0.03f, uy = 0.0f;
+    const R rho = (f[0] + f[3] + f[4] + f[6] + f[7]) / (1.0f - ux - uy);
+    f[1] = f[3] + (2.0f / 3.0f) * rho * ux;
+    f[2] = f[4];
+    f[5] = f[7] + (1.0f / 6.0f) * rho * (ux + uy);
+    f[8] = f[6] + (1.0f / 6.0f) * rho * (ux - uy);
+}
+template <typename R>
+__device__ __forceinline__ void bc_corner_bottom_left(R f[9]) {
+    const float ux = 0.03f, uy = 0.0f;
+    const R rho = (f[0] + f[2] + f[3] + f[5] + f[6]) / (1.0f - ux + uy);
+    f[1] = f[3] + (2.0f / 3.0f) * rho * ux;
+    f[4] = f[2];
+    f[5] = f[7] + (1.0f / 6.0f) * rho * (ux + uy);
+    f[8] = f[6] + (1.0f / 6.0f) * rho * (ux - uy);
+}
+
 // Dispatch on the node's flag (boundaries_kernel_2D, boundaries.cuh:10-85).
 __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, int y, uint8_t fl) {
     const Geometry& g = a.g;
@@ -550,6 +574,8 @@ __device__ __forceinline__ void apply_bc(const StepArgs& a, float f[9], int x, i
         break;
     case LBMX_ZOU_HE_PRESSURE_RIGHT: bc_zouhe_pressure_right(f, a.rho_out_bc); break;
     case LBMX_ZOU_HE_PARABOLIC_LEFT: bc_zouhe_left(f, parabolic_ux(a.u_bc, y, g.ny), false); break;
+    case LBMX_CORNER_TOP_LEFT: bc_corner_top_left(f); break;
+    case LBMX_CORNER_BOTTOM_LEFT: bc_corner_bottom_left(f); break;
     default: break;  // half-way walls act in load/store; unknown flags are left alone as the reference does
     }
 }

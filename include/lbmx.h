@@ -48,8 +48,9 @@ enum { LBMX_BGK = 0, LBMX_MRT = 1, LBMX_CM = 2, LBMX_CM_OPT = 3 };
 enum { LBMX_STORAGE_F32 = 0, LBMX_STORAGE_F16_OFFSET = 1, LBMX_STORAGE_BF16_OFFSET = 2 };
 
 /* Boundary flags.  0..12 keep the values of the reference's BC_flag
- * (src/core/lbm_constants.cuh:376-396); 32.. are boundaries the reference
- * does not have. */
+ * (src/core/lbm_constants.cuh:376-396); 32..35 are boundaries the reference
+ * does not have; 36..37 are reference functors that its 2-D boundary kernel
+ * never dispatches (no BC_flag selects them). */
 enum {
     LBMX_FLUID = 0,
     LBMX_BOUNCE_BACK = 1,            /* BounceBack<2>, bbDomainBoundary.cuh:14-50 */
@@ -67,7 +68,9 @@ enum {
     LBMX_MOVING_WALL_BB = 32,        /* half-way bounce-back with wall velocity (wall_ux, wall_uy) */
     LBMX_ZOU_HE_PRESSURE_RIGHT = 33, /* Zou-He pressure outlet at x = nx-1, density rho_out */
     LBMX_ZOU_HE_PARABOLIC_LEFT = 34, /* Zou-He velocity inlet at x = 0, parabolic profile of peak u_bc */
-    LBMX_HALFWAY_BB = 35             /* stationary half-way bounce-back */
+    LBMX_HALFWAY_BB = 35,            /* stationary half-way bounce-back */
+    LBMX_CORNER_TOP_LEFT = 36,       /* CornerBoundary::apply_top_left, cornerBoundaries.cuh:39-59 (ux = 0.03) */
+    LBMX_CORNER_BOTTOM_LEFT = 37     /* CornerBoundary::apply_bottom_left, cornerBoundaries.cuh:61-81 (ux = 0.03) */
 };
 
 /* Switches that reproduce the reference's as-shipped behaviour. */

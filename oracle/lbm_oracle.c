@@ -339,6 +339,28 @@ static void bc_aux(lbo* o, int x, int y, real* aux) {
     }
 }
 
+/* CornerBoundary::apply_top_left / apply_bottom_left
+ * (src/functors/boundaryConditions/cornerBoundaries.cuh:39-59, 61-81): the
+ * corners of a left inlet whose velocity is fixed at ux = 0.03, uy = 0; the
+ * top-left one sets f2 from f4, the bottom-left one f4 from f2, as there. */
+static void bc_corner_top_left(real* f) {
+    const real ux = (real)0.03f, uy = 0;
+    real rho = (f[0] + f[3] + f[4] + f[6] + f[7]) / ((real)1 - ux - uy);
+    f[1] = f[3] + ((real)2 / 3) * rho * ux;
+    f[2] = f[4];
+    f[5] = f[7] + ((real)1 / 6) * rho * (ux + uy);
+    f[8] = f[6] + ((real)1 / 6) * rho * (ux - uy);
+}
+
+static void bc_corner_bottom_left(real* f) {
+    const real ux = (real)0.03f, uy = 0;
+    real rho = (f[0] + f[2] + f[3] + f[5] + f[6]) / ((real)1 - ux + uy);
+    f[1] = f[3] + ((real)2 / 3) * rho * ux;
+    f[4] = f[2];
+    f[5] = f[7] + ((real)1 / 6) * rho * (ux + uy);
+    f[8] = f[6] + ((real)1 / 6) * rho * (ux - uy);
+}
+
 static void apply_bc(const lbo* o, real* f, int x, int y, uint8_t fl, const real* aux) {
     switch (fl) {
     case LBO_FLUID: break;
@@ -373,6 +395,8 @@ static void apply_bc(const lbo* o, real* f, int x, int y, uint8_t fl, const real
         bc_zouhe_left(f, ux, 0);
         break;
     }
+    case LBO_CORNER_TOP_LEFT: bc_corner_top_left(f); break;
+    case LBO_CORNER_BOTTOM_LEFT: bc_corner_bottom_left(f); break;
     default: break; /* the reference prints "Unknown Flag" and leaves the node alone */
     }
 }

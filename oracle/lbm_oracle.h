@@ -52,7 +52,8 @@ enum {
 };
 
 /* boundary flags: values 0..12 are the reference's BC_flag (lbm_constants.cuh:376-396);
- * 32.. are boundaries the reference does not have. */
+ * 32..35 are boundaries the reference does not have; 36..37 are reference
+ * functors its 2-D boundary kernel never dispatches (CornerBoundary). */
 enum {
     LBO_FLUID = 0, LBO_BOUNCE_BACK = 1, LBO_ZOU_HE_TOP = 2, LBO_ZOU_HE_LEFT = 3,
     LBO_ZOU_HE_TOP_LEFT_TOP_INFLOW = 4, LBO_ZOU_HE_TOP_RIGHT_TOP_INFLOW = 5,
@@ -60,7 +61,7 @@ enum {
     LBO_REGULARIZED_INLET_TOP = 9, LBO_REGULARIZED_INLET_LEFT = 10,
     LBO_REGULARIZED_BOUNCE_BACK = 11, LBO_REGULARIZED_BOUNCE_BACK_CORNER = 12,
     LBO_MOVING_WALL_BB = 32, LBO_ZOU_HE_PRESSURE_RIGHT = 33, LBO_ZOU_HE_PARABOLIC_LEFT = 34,
-    LBO_HALFWAY_BB = 35
+    LBO_HALFWAY_BB = 35, LBO_CORNER_TOP_LEFT = 36, LBO_CORNER_BOTTOM_LEFT = 37
 };
 
 typedef struct lbo_params {

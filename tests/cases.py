@@ -13,6 +13,7 @@ FLUID, BOUNCE_BACK, ZOU_HE_TOP, ZOU_HE_LEFT = 0, 1, 2, 3
 CYLINDER, ZG_OUTFLOW, PRESSURE_OUTLET, REGULARIZED_INLET_TOP = 6, 7, 8, 9
 REGULARIZED_BOUNCE_BACK, REGULARIZED_BOUNCE_BACK_CORNER = 11, 12
 MOVING_WALL_BB, ZOU_HE_PRESSURE_RIGHT, ZOU_HE_PARABOLIC_LEFT, HALFWAY_BB = 32, 33, 34, 35
+CORNER_TOP_LEFT, CORNER_BOTTOM_LEFT = 36, 37
 QUIRKS_REFERENCE = 0x1F
 
 

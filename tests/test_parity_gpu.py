@@ -147,6 +147,18 @@ def test_channel_parabolic_zouhe_pressure():
     compare(o, L)
 
 
+@pytest.mark.parametrize("op", [C.BGK, C.MRT])
+def test_channel_reference_corner_boundaries(op):
+    # CornerBoundary (cornerBoundaries.cuh:38-82) at the inlet's two corners:
+    # a uniform Zou-He inlet at the corners' fixed ux = 0.03; own-node rules
+    # on populations that partly come from the edge store
+    c = C.random_state(C.channel(96, 48, op=op, u_in=0.03), seed=13)
+    c["flags"][0, 0] = C.CORNER_BOTTOM_LEFT
+    c["flags"][-1, 0] = C.CORNER_TOP_LEFT
+    o, L = run_both(c, 151)
+    compare(o, L)
+
+
 @pytest.mark.parametrize("quirks", [0, C.QUIRKS_REFERENCE])
 def test_channel_ibm_cylinder(quirks):
     mk = C.cylinder_markers(32.3, 24.1, 6.0, 32)
@@ -263,6 +275,9 @@ def test_flag_validation():
         L.set_flags(bad)
     assert e.value.code == 4
     bad[3, 3] = 200
+    with pytest.raises(lbmx.LbmxError):
+        L.set_flags(bad)
+    bad[3, 3] = C.CORNER_BOTTOM_LEFT + 1  # one past the last flag
     with pytest.raises(lbmx.LbmxError):
         L.set_flags(bad)
     bad[:] = 0
