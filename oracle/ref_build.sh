@@ -1,12 +1,16 @@
 #!/bin/bash
-# Recipe for the reference's own 2-D build, used only to make golden vectors
-# (test infrastructure; nothing in the product links it).
+# Recipe for the reference's own 2-D build, used to make golden vectors and to
+# time the reference's GPU step (test infrastructure; nothing in the product
+# links it).
 #
 #   ref_build.sh sources   copy src/ and third_party/ of the reference checkout
 #                          into oracle/_ref/ and patch the COPY so the D2Q9
 #                          path compiles (the checkout is never modified)
 #   ref_build.sh build     compile oracle/ref_harness.cu against the patched
 #                          copy, one binary per golden case, into oracle/_ref/bin/
+#   ref_build.sh timers    compile oracle/ref_timer.cu the same way, one binary
+#                          per timed configuration (oracle/_ref/bin/time_*), to
+#                          time the reference's own GPU step
 #
 # oracle/_ref/ is git-ignored; it travels with the working tree, so `build`
 # also works where the reference checkout is absent.  The patches are the
@@ -76,6 +80,13 @@ CASES=(
   "channel_pressure_cm|-DNX=48 -DNY=24 -DLBX_CASE=5 -DLBX_OPID=2 -DLBX_NU=0.04f"
 )
 
+# timed configurations | -D flags: the 1024^2 lid-driven cavity (MRT, Re 1000,
+# the reference's regularized walls) and the 256^2 Taylor-Green vortex (BGK)
+TIMERS=(
+  "time_cavity1024_mrt|-DNX=1024 -DNY=1024 -DLBX_CASE=2 -DLBX_OPID=1 -DLBX_NU=0.1024f"
+  "time_tg256_bgk|-DNX=256 -DNY=256 -DPERIODIC_X -DPERIODIC_Y -DLBX_CASE=1 -DLBX_OPID=0 -DLBX_NU=0.01f"
+)
+
 build() {
     local S=$OUT/src
     [ -d "$S" ] || { echo "no patched sources in $OUT/src (run: ref_build.sh sources)"; exit 1; }
@@ -85,15 +96,18 @@ build() {
 $S/core/equilibrium/equilibrium.cu $S/core/collision/MRT/MRT.cu $S/core/collision/CM/CM.cu \
 $S/IBM/IBM_impl.cu $S/IBM/IBM_generators.cu $S/util/utility.cu"
     local pids=()
-    for c in "${CASES[@]}"; do
+    local driver=$HERE/ref_harness.cu
+    local list=("${CASES[@]}")
+    if [ "${1:-}" = timers ]; then driver=$HERE/ref_timer.cu; list=("${TIMERS[@]}"); fi
+    for c in "${list[@]}"; do
         local name=${c%%|*} defs=${c#*|}
-        ( $NVCC $FLAGS $defs "$HERE/ref_harness.cu" $SRCS -o "$OUT/bin/$name" > "$OUT/obj/$name.log" 2>&1 \
+        ( $NVCC $FLAGS $defs "$driver" $SRCS -o "$OUT/bin/$name" > "$OUT/obj/$name.log" 2>&1 \
           || { echo "build of $name failed:"; tail -30 "$OUT/obj/$name.log"; exit 1; } ) &
         pids+=($!)
     done
     local rc=0
     for p in "${pids[@]}"; do wait "$p" || rc=1; done
-    [ $rc -eq 0 ] && echo "built ${#CASES[@]} reference harness binaries in $OUT/bin"
+    [ $rc -eq 0 ] && echo "built ${#list[@]} reference binaries in $OUT/bin"
     return $rc
 }
 
@@ -102,6 +116,7 @@ list() { for c in "${CASES[@]}"; do echo "${c%%|*}|${c#*|}"; done; }
 case "${1:-}" in
     sources) sources ;;
     build) build ;;
+    timers) build timers ;;
     list) list ;;
-    *) echo "usage: $0 sources|build|list"; exit 2 ;;
+    *) echo "usage: $0 sources|build|timers|list"; exit 2 ;;
 esac
