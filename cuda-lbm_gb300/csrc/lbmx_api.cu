@@ -291,8 +291,13 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     if (!p) return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: params is NULL");
     if (p->nx < 3 || p->ny < 3)
         return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: nx, ny must be >= 3 (got %d x %d)", p->nx, p->ny);
-    if ((long long)p->nx * p->ny > (1LL << 31) - 1)
-        return fail(nullptr, LBMX_ERR_TOO_LARGE, "lbmx_create: %d x %d nodes exceeds 2^31-1", p->nx, p->ny);
+    // node offsets y * pitch + x are 32-bit in the work lists and tiles, so
+    // the plane with its rows padded to whole tiles must fit
+    const long long padded_plane = (long long)p->ny * (((long long)p->nx + kStageW - 1) / kStageW * kStageW);
+    if (padded_plane > (1LL << 31) - 1)
+        return fail(nullptr, LBMX_ERR_TOO_LARGE,
+                    "lbmx_create: %d x %d nodes (%lld with rows padded to whole %d-node tiles) exceeds 2^31-1",
+                    p->nx, p->ny, padded_plane, kStageW);
     if (p->op < LBMX_BGK || p->op > LBMX_CM_OPT)
         return fail(nullptr, LBMX_ERR_INVALID_ARGUMENT, "lbmx_create: unknown operator %d", p->op);
     if (p->storage < LBMX_STORAGE_F32 || p->storage > LBMX_STORAGE_BF16_OFFSET)

@@ -37,3 +37,19 @@ def test_version_and_defaults_without_gpu():
     lib.lbmx_params_default(ctypes.byref(p))
     assert p.op == 0 and p.storage == 0 and p.ibm_iters == 3 and abs(p.rho_out - 1) < 1e-7
     assert ctypes.sizeof(lbmx.Params) == 4 * 10 + 4 * 17 + 4 + 8  # matches the C struct
+
+
+def test_create_rejects_lattices_whose_padded_plane_overflows():
+    # rows are padded to whole 128-node tiles and node offsets are 32-bit:
+    # 129 x 16,646,000 nodes fit in 2^31 but their padded plane (256 per row)
+    # does not.  The size checks come before any device call.
+    import lbmx
+    lib = lbmx.load_library(B.build())
+    for nx, ny in ((129, 16646000), (1 << 16, 1 << 16)):
+        p = lbmx.Params()
+        lib.lbmx_params_default(ctypes.byref(p))
+        p.nx, p.ny = nx, ny
+        h = ctypes.c_void_p()
+        assert lib.lbmx_create(ctypes.byref(p), ctypes.byref(h)) == 8  # LBMX_ERR_TOO_LARGE
+        assert not h.value
+
