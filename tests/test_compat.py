@@ -2,7 +2,11 @@
 
 * CPU: the reference's own unchanged 2-D scenario headers (Taylor-Green,
   lid-driven cavity, Poiseuille) compile against cuda-lbm_gb300/compat,
-  including their compute_error validators.
+  including their compute_error validators.  The flow-past-cylinder header
+  does not compile as shipped, against the reference's own headers either
+  (its ScenarioTrait names the template BGK without <2>,
+  flowPastCylinderScenario.cuh:12); with that one token fixed, in a
+  temporary copy, it compiles too.
 * GPU: the golden scenarios (oracle/ref_scenarios.cuh) -- the very source the
   reference's build ran to write tests/golden/ -- run on lbmx through
   lbmx_compat::create and reproduce the reference's dumps.
@@ -33,17 +37,36 @@ UNCHANGED = [
 @pytest.mark.skipif(not os.path.isdir(REF_SCEN), reason="reference checkout not mounted")
 @pytest.mark.parametrize("header,name,defs", UNCHANGED, ids=[u[1] for u in UNCHANGED])
 def test_reference_scenario_headers_compile_unchanged(header, name, defs, tmp_path):
+    _compile_scenario(os.path.join(REF_SCEN, header), name, defs, tmp_path)
+
+
+def _compile_scenario(header_path, name, defs, tmp_path, extra_includes=()):
     src = tmp_path / "use_scenario.cu"
     src.write_text(
         '#include "lbmx_scenario.cuh"\n'
-        '#include "%s/%s"\n'
+        '#include "%s"\n'
         "int build(lbmx_handle** h) { return lbmx_compat::create<%s>(h); }\n"
         "float validate() { lbmx_compat::Solver<%s> s; s.step(1); return %s::compute_error(s); }\n"
-        % (REF_SCEN, header, name, name, name))
-    cmd = ["nvcc"] + ARCH + ["-std=c++17", "-c", "-w", "-I" + COMPAT, "-I" + INCLUDE] + defs.split() + \
-        [str(src), "-o", str(tmp_path / "use_scenario.o")]
+        % (header_path, name, name, name))
+    cmd = ["nvcc"] + ARCH + ["-std=c++17", "-c", "-w", "-I" + COMPAT, "-I" + INCLUDE] + \
+        ["-I" + d for d in extra_includes] + defs.split() + [str(src), "-o", str(tmp_path / "use_scenario.o")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SCEN), reason="reference checkout not mounted")
+def test_reference_cylinder_scenario_compiles_with_its_template_argument_fixed(tmp_path):
+    # the one change the reference's own build needs too: `BGK` -> `BGK<2>`
+    # in the ScenarioTrait argument list; the functors header is used as is
+    d = os.path.join(REF_SCEN, "flowPastCylinder")
+    text = open(os.path.join(d, "flowPastCylinderScenario.cuh"), newline="").read().replace("\r\n", "\n")
+    lines = text.split("\n")
+    fixed = [i for i, ln in enumerate(lines) if ln.strip() == "BGK"]
+    assert len(fixed) == 1
+    lines[fixed[0]] = lines[fixed[0]].replace("BGK", "BGK<2>")
+    copy = tmp_path / "flowPastCylinderScenario.cuh"
+    copy.write_text("\n".join(lines))
+    _compile_scenario(str(copy), "FlowPastCylinderScenario", "-DNX=400 -DNY=100", tmp_path, extra_includes=(d,))
 
 
 def _case_flags(name):
