@@ -96,6 +96,10 @@ __global__ void __launch_bounds__(kNaThreads) moment_sums_kernel(const float* __
 // Device address of the scratch array, looked up once per device.  A host
 // pointer to g_noalloc_scratch is only a stand-in for the symbol; kernels must
 // be given the address cudaGetSymbolAddress returns for the current device.
+// The cached address belongs to the device's primary context (the one the
+// runtime API uses) and stays valid until that context is destroyed: a
+// process that calls cudaDeviceReset, or that makes another driver context
+// current on the device, must not call this entry point afterwards.
 constexpr int kNaMaxDevices = 64;
 std::mutex g_na_mutex;
 double* g_na_addr[kNaMaxDevices] = {};
@@ -151,8 +155,16 @@ lbmx_status lbmx_moment_sums_noalloc(const float* rho, const float* u, int64_t n
     if (e != cudaSuccess) return na_fail(LBMX_ERR_CUDA, "lbmx_moment_sums_noalloc: launch", e);
     e = cudaMemcpyAsync(sums3, s.result, 3 * sizeof(double), cudaMemcpyDefault, st);
     if (e != cudaSuccess) return na_fail(LBMX_ERR_CUDA, "lbmx_moment_sums_noalloc: copying the result", e);
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return na_fail(LBMX_ERR_CUDA, "lbmx_moment_sums_noalloc: synchronize", e);
+    // Only pageable host memory makes the call wait: its caller reads the
+    // sums as soon as the call returns.  Device, managed and page-locked
+    // host memory receive them in stream order, so the host is not blocked.
+    cudaPointerAttributes pa;
+    e = cudaPointerGetAttributes(&pa, sums3);
+    if (e != cudaSuccess) return na_fail(LBMX_ERR_CUDA, "lbmx_moment_sums_noalloc: classifying sums3", e);
+    if (pa.type == cudaMemoryTypeUnregistered) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return na_fail(LBMX_ERR_CUDA, "lbmx_moment_sums_noalloc: synchronize", e);
+    }
     return LBMX_OK;
 }
 

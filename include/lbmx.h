@@ -242,7 +242,10 @@ const char* lbmx_last_error(lbmx_handle* h);
 /* No counterpart in the reference.  FP64 sums {rho, rho*ux, rho*uy} over n
  * nodes of caller-owned device fields rho[n] and u[2n] (x plane, then y
  * plane) into sums3 (host or device memory), on `stream` (a cudaStream_t;
- * NULL = legacy default stream); returns after the result has arrived.
+ * NULL = legacy default stream).  When sums3 is pageable host memory the call
+ * returns after the sums have arrived.  Otherwise (device, managed or
+ * page-locked host memory) the host is not blocked: the sums are there once
+ * `stream` has reached this call's work.
  *
  * For callers that may not allocate device memory where they need the sums:
  * between steps of a loop that must not stall the GPU (cudaMalloc and
@@ -254,7 +257,9 @@ const char* lbmx_last_error(lbmx_handle* h);
  *
  * n above LBMX_NOALLOC_MAX_NODES returns LBMX_ERR_TOO_LARGE.  The first call
  * on a device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  All calls on a device
+ * make that first call before any stream capture.  That address is kept for
+ * the device's primary context: do not call this after cudaDeviceReset or
+ * with another driver context current on the device.  All calls on a device
  * share the array: calls whose work can overlap on the GPU (different
  * streams with no ordering between them) race and must not be made. */
 #define LBMX_NOALLOC_MAX_NODES 2147483647LL
