@@ -242,11 +242,11 @@ void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
 }
 
 static void free_ibm(lbmx_handle* h) {
-    cudaFree(h->patch_nodes); cudaFree(h->sten_idx); cudaFree(h->sten_w);
-    cudaFree(h->patch_rho); cudaFree(h->patch_u); cudaFree(h->marker_u);
+    cudaFree(h->patch_nodes); cudaFree(h->sten_idx); cudaFree(h->sten_w); cudaFree(h->spread);
+    cudaFree(h->marker_u);
     cudaFree(h->marker_rho); cudaFree(h->marker_force); cudaFree(h->ibm_force);
-    h->patch_nodes = nullptr; h->sten_idx = nullptr; h->sten_w = nullptr;
-    h->patch_rho = h->patch_u = h->marker_u = h->marker_rho = h->marker_force = h->ibm_force = nullptr;
+    h->patch_nodes = nullptr; h->sten_idx = nullptr; h->sten_w = nullptr; h->spread = nullptr;
+    h->marker_u = h->marker_rho = h->marker_force = h->ibm_force = nullptr;
     h->nm = h->npatch = 0;
     h->patch_host.clear();
 }
@@ -532,16 +532,15 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, b
     if (h->has_aux_bc)
         LBMX_CUDA(h, dispatch(storage, [&](auto tag) { return launch_edge_prepass<decltype(tag)>(a, h->aux, st); }));
     if (h->nm > 0) {
-        IbmArgs ia;
+        IbmArgs ia{};
         ia.nm = h->nm;
         ia.npatch = h->npatch;
         ia.iters = h->p.ibm_iters;
         ia.stencil = h->stencil;
         ia.sten_idx = h->sten_idx;
         ia.sten_w = h->sten_w;
+        ia.spread = h->spread;
         ia.patch_nodes = h->patch_nodes;
-        ia.patch_rho = h->patch_rho;
-        ia.patch_u = h->patch_u;
         ia.marker_u = h->marker_u;
         ia.marker_rho = h->marker_rho;
         ia.marker_force = h->marker_force;
@@ -550,7 +549,7 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, b
         ia.clamp = (h->p.quirks & LBMX_QUIRK_IBM_CLAMP) ? 1 : 0;
         ia.ds = h->p.ibm_ds;
         LBMX_CUDA(h, dispatch(storage, [&](auto tag) {
-                      return launch_ibm_step<decltype(tag)>(a, ia, h->patch_rho, h->patch_u, st);
+                      return launch_ibm_step<decltype(tag)>(a, ia, st);
                   }));
     }
     const bool opt = h->p.op == LBMX_CM_OPT;
@@ -792,6 +791,18 @@ int ibm_build_stencil(int nx, int ny, long long pitch, bool two, const float* hx
     }
     return -1;
 }
+
+std::vector<int> ibm_build_spread(int np, const std::vector<int>& sidx) {
+    std::vector<int> sp((size_t)np + 1, 0);
+    for (int idx : sidx)
+        if (idx >= 0) sp[(size_t)idx + 1]++;
+    for (int i = 0; i < np; i++) sp[(size_t)i + 1] += sp[(size_t)i];
+    sp.resize((size_t)np + 1 + (size_t)sp[(size_t)np]);
+    std::vector<int> fill(sp.begin(), sp.begin() + np);
+    for (size_t j = 0; j < sidx.size(); j++)
+        if (sidx[j] >= 0) sp[(size_t)np + 1 + (size_t)fill[(size_t)sidx[j]]++] = (int)j;
+    return sp;
+}
 }  // namespace lbmx
 
 extern "C" {
@@ -822,8 +833,6 @@ lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
     LBMX_CUDA(h, cudaMalloc((void**)&h->patch_nodes, np * sizeof(int)));
     LBMX_CUDA(h, cudaMalloc((void**)&h->sten_idx, (size_t)n * S2 * sizeof(int)));
     LBMX_CUDA(h, cudaMalloc((void**)&h->sten_w, (size_t)n * S2 * sizeof(float)));
-    LBMX_CUDA(h, cudaMalloc((void**)&h->patch_rho, np * sizeof(float)));
-    LBMX_CUDA(h, cudaMalloc((void**)&h->patch_u, 2 * (size_t)np * sizeof(float)));
     LBMX_CUDA(h, cudaMalloc((void**)&h->marker_u, 2 * (size_t)n * sizeof(float)));
     LBMX_CUDA(h, cudaMalloc((void**)&h->marker_rho, (size_t)n * sizeof(float)));
     LBMX_CUDA(h, cudaMalloc((void**)&h->marker_force, 2 * (size_t)n * sizeof(float)));
@@ -831,6 +840,9 @@ lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
     LBMX_CUDA(h, cudaMemcpy(h->patch_nodes, nodes.data(), np * sizeof(int), cudaMemcpyHostToDevice));
     LBMX_CUDA(h, cudaMemcpy(h->sten_idx, sidx.data(), sidx.size() * sizeof(int), cudaMemcpyHostToDevice));
     LBMX_CUDA(h, cudaMemcpy(h->sten_w, sw.data(), sw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    const std::vector<int> spread = lbmx::ibm_build_spread(np, sidx);
+    LBMX_CUDA(h, cudaMalloc((void**)&h->spread, spread.size() * sizeof(int)));
+    LBMX_CUDA(h, cudaMemcpy(h->spread, spread.data(), spread.size() * sizeof(int), cudaMemcpyHostToDevice));
     LBMX_CUDA(h, cudaMemset(h->ibm_force, 0, 2 * (size_t)g.plane * sizeof(float)));
     LBMX_CUDA(h, cudaMemset(h->marker_force, 0, 2 * (size_t)n * sizeof(float)));
     LBMX_CUDA(h, cudaMemset(h->marker_u, 0, 2 * (size_t)n * sizeof(float)));

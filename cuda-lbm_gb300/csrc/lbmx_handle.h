@@ -41,8 +41,7 @@ struct lbmx_handle {
     int* patch_nodes = nullptr;
     int* sten_idx = nullptr;
     float* sten_w = nullptr;
-    float* patch_rho = nullptr;
-    float* patch_u = nullptr;
+    int* spread = nullptr;         // spread lists of the patch nodes (IbmData::spread)
     float* marker_u = nullptr;
     float* marker_rho = nullptr;
     float* marker_force = nullptr;
@@ -83,6 +82,10 @@ bool encode_population_map(const lbmx_handle* h, CUtensorMap* out, int tile_w, i
 // Returns -1, or the index of the first non-finite marker.
 int ibm_build_stencil(int nx, int ny, long long pitch, bool two_by_two, const float* xy, int n,
                       std::vector<int>& sidx, std::vector<float>& sw, std::vector<int>& nodes);
+// Spread lists of a stencil over np patch nodes: [np + 1] offsets, then for
+// each patch node the stencil points (indices into sidx) that touch it, in
+// ascending order.
+std::vector<int> ibm_build_spread(int np, const std::vector<int>& sidx);
 
 template <typename Fn>
 cudaError_t dispatch(int storage, Fn fn) {

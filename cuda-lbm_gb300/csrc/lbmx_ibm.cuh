@@ -16,13 +16,6 @@ namespace lbmx {
 
 constexpr int kIbmThreads = 1024;
 
-__device__ __forceinline__ void ibm_atomic_add(float* p, float v) { atomicAdd(p, v); }
-template <int K>
-__device__ __forceinline__ void ibm_atomic_add(Dual<K>* p, const Dual<K>& v) {
-    atomicAdd(&p->v, v.v);
-#pragma unroll
-    for (int k = 0; k < K; k++) atomicAdd(&p->d[k], v.d[k]);
-}
 // the reference's clamps (IBM_impl.cuh:22-24, 42-44)
 __device__ __forceinline__ float ibm_clamp(float x) { return x > 1e-8f ? x : 0.0f; }
 template <int K>
@@ -38,63 +31,99 @@ __device__ __forceinline__ Dual<K> ibm_shfl_xor(const Dual<K>& x, int o) {
     return r;
 }
 
-// patch and marker state, then the stencils (index and weight per point)
+// Shared-memory state of the rounds: patch and marker values, then the
+// stencils (index and weight per point) and the spread lists (for each patch
+// node, the stencil points that touch it, in ascending order).
 template <typename R>
 size_t ibm_smem_bytes_of(int npatch, int nm, int stencil) {
-    return (size_t)(8 * npatch + 4 * nm) * sizeof(R) + (size_t)nm * stencil * stencil * (sizeof(int) + sizeof(float));
+    const size_t s2 = (size_t)stencil * stencil;
+    return (size_t)(6 * npatch + 4 * nm) * sizeof(R) + (size_t)nm * s2 * (sizeof(int) + sizeof(float)) +
+           ((size_t)npatch + 1 + (size_t)nm * s2) * sizeof(int);
 }
 
-// All rounds of one step in one CTA; sm holds ibm_smem_bytes_of<R> bytes.
-// The stencils are staged in shared memory once; each interpolation gives
-// every stencil point its own thread and sums a marker's points with a fixed
-// shuffle tree (S2 = stencil^2 = 4 or 16 points, consecutive in one warp).
+template <typename R>
+struct IbmSmem {
+    R *upx, *upy, *rho, *half_inv;  // working velocity (u_prev of the reference), density, 1 / (2 rho)
+    R *ftx, *fty;                   // Eulerian force summed over rounds
+    R *mfx, *mfy, *mtx, *mty;       // marker force of this round and summed over rounds
+    int* sidx;                      // [nm * S2] patch index or -1
+    float* sw;                      // [nm * S2] kernel weight
+    int* sp;                        // [npatch + 1] offsets into spj
+    int* spj;                       // stencil points of each patch node
+};
+
+template <typename R>
+__device__ __forceinline__ IbmSmem<R> ibm_layout(const IbmData<R>& a, R* sm) {
+    const int np = a.npatch, nm = a.nm, nj = nm * a.stencil * a.stencil;
+    IbmSmem<R> s;
+    s.upx = sm;
+    s.upy = s.upx + np;
+    s.rho = s.upy + np;
+    s.half_inv = s.rho + np;
+    s.ftx = s.half_inv + np;
+    s.fty = s.ftx + np;
+    s.mfx = s.fty + np;
+    s.mfy = s.mfx + nm;
+    s.mtx = s.mfy + nm;
+    s.mty = s.mtx + nm;
+    s.sidx = reinterpret_cast<int*>(s.mty + nm);
+    s.sw = reinterpret_cast<float*>(s.sidx + nj);
+    s.sp = reinterpret_cast<int*>(s.sw + nj);
+    s.spj = s.sp + np + 1;
+    return s;
+}
+
+// Stage what does not depend on the flow (stencils, spread lists) and clear
+// the accumulators; no barrier (the caller syncs before the rounds).
+template <typename R>
+__device__ void ibm_stage(const IbmData<R>& a, const IbmSmem<R>& s) {
+    const int np = a.npatch, nm = a.nm, nj = nm * a.stencil * a.stencil;
+    const R zero = splat(0.0f, R{});
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) {
+        s.sidx[j] = a.sten_idx[j];
+        s.sw[j] = a.sten_w[j];
+    }
+    const int nsp = a.spread[np];
+    for (int j = threadIdx.x; j < np + 1 + nsp; j += blockDim.x) s.sp[j] = a.spread[j];
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s.ftx[i] = s.fty[i] = zero;
+    for (int k = threadIdx.x; k < nm; k += blockDim.x) s.mtx[k] = s.mty[k] = zero;
+}
+
+// Patch density and uncorrected velocity of patch node i.
+template <typename R>
+__device__ __forceinline__ void ibm_set_patch(const IbmSmem<R>& s, int i, R rho, R ux, R uy) {
+    s.rho[i] = rho;
+    s.half_inv[i] = 1.0f / (2.0f * rho);
+    s.upx[i] = ux;
+    s.upy[i] = uy;
+}
+
+// All rounds of one step on the staged patch (ibm_stage, ibm_set_patch and a
+// barrier before).  Each interpolation gives every stencil point its own
+// thread and sums a marker's points with a fixed shuffle tree (S2 = stencil^2
+// = 4 or 16 points, consecutive in one warp).  The spread gives every patch
+// node a thread that adds the forces of the stencil points touching it in
+// ascending order, so the result is the same bit for bit on every run, and
+// applies the velocity correction in the same pass.
 template <typename R, int S2>
-__device__ void ibm_rounds_s(const IbmData<R>& a, R* sm) {
+__device__ void ibm_iterate_s(const IbmData<R>& a, const IbmSmem<R>& s) {
     const int np = a.npatch, nm = a.nm;
     const R zero = splat(0.0f, R{});
-    R* upx = sm;            // working velocity (u_prev of the reference)
-    R* upy = upx + np;
-    R* rho = upy + np;
-    R* fix = rho + np;      // this round's spread force
-    R* fiy = fix + np;
-    R* ftx = fiy + np;      // force summed over rounds
-    R* fty = ftx + np;
-    R* mfx = fty + np;      // marker force of this round
-    R* mfy = mfx + nm;
-    R* mtx = mfy + nm;      // marker force summed over rounds
-    R* mty = mtx + nm;
-    R* half_inv = mty + nm;  // 1 / (2 rho) of each patch node (rho is fixed over the rounds)
-    int* sidx = reinterpret_cast<int*>(half_inv + np);
-    float* sw = reinterpret_cast<float*>(sidx + nm * S2);
     const int tid = threadIdx.x;
     const int nj = nm * S2;
-    for (int j = tid; j < nj; j += blockDim.x) {
-        sidx[j] = a.sten_idx[j];
-        sw[j] = a.sten_w[j];
-    }
-    for (int i = tid; i < np; i += blockDim.x) {
-        upx[i] = a.patch_u[i];
-        upy[i] = a.patch_u[np + i];
-        rho[i] = a.patch_rho[i];
-        half_inv[i] = 1.0f / (2.0f * rho[i]);
-        ftx[i] = zero;
-        fty[i] = zero;
-    }
-    for (int k = tid; k < nm; k += blockDim.x) mtx[k] = mty[k] = zero;
-    __syncthreads();
     for (int it = 0; it < a.iters; it++) {
-        for (int i = tid; i < np; i += blockDim.x) fix[i] = fiy[i] = zero;
+        const bool last = it == a.iters - 1;
         // interpolate_velocities_kernel<2> (IBM_impl.cu:5-51) then
         // compute_lagrangian_kernel (IBM_impl.cuh:7-26), target velocity 0
         for (int j0 = 0; j0 < nj; j0 += blockDim.x) {
             const int j = j0 + tid;
             R r = zero, ux = zero, uy = zero;
-            const int idx = j < nj ? sidx[j] : -1;
+            const int idx = j < nj ? s.sidx[j] : -1;
             if (idx >= 0) {
-                const float w = sw[j];
-                r = w * rho[idx];
-                ux = w * upx[idx];
-                uy = w * upy[idx];
+                const float w = s.sw[j];
+                r = w * s.rho[idx];
+                ux = w * s.upx[idx];
+                uy = w * s.upy[idx];
             }
             for (int o = S2 >> 1; o > 0; o >>= 1) {
                 r = r + ibm_shfl_xor(r, o);
@@ -109,58 +138,68 @@ __device__ void ibm_rounds_s(const IbmData<R>& a, R* sm) {
                 fx = ibm_clamp(fx);
                 fy = ibm_clamp(fy);
             }
-            mfx[k] = fx;
-            mfy[k] = fy;
-            mtx[k] = mtx[k] + fx;
-            mty[k] = mty[k] + fy;
-            if (it == a.iters - 1) {
+            s.mfx[k] = fx;
+            s.mfy[k] = fy;
+            const R tx = s.mtx[k] + fx, ty = s.mty[k] + fy;
+            s.mtx[k] = tx;
+            s.mty[k] = ty;
+            if (last) {
                 a.marker_u[k] = ux;
                 a.marker_u[nm + k] = uy;
                 a.marker_rho[k] = r;
+                a.marker_force[k] = tx;
+                a.marker_force[nm + k] = ty;
             }
         }
         __syncthreads();
-        // spread_forces_kernel<2> (IBM_impl.cu:120-154)
-        for (int j = tid; j < nj; j += blockDim.x) {
-            const int k = j / S2;
-            const int idx = sidx[j];
-            if (idx < 0) continue;
-            const float w = sw[j] * a.ds;
-            ibm_atomic_add(&fix[idx], w * mfx[k]);
-            ibm_atomic_add(&fiy[idx], w * mfy[k]);
-        }
-        __syncthreads();
+        // spread_forces_kernel<2> (IBM_impl.cu:120-154), then
         // correct_velocities_kernel + accumulate_forces_kernel (IBM_impl.cuh:28-68)
         for (int i = tid; i < np; i += blockDim.x) {
-            R cx = upx[i] + fix[i] * half_inv[i];
-            R cy = upy[i] + fiy[i] * half_inv[i];
+            R fx = zero, fy = zero;
+            const int e1 = s.sp[i + 1];
+            for (int e = s.sp[i]; e < e1; e++) {
+                const int j = s.spj[e];
+                const float w = s.sw[j] * a.ds;
+                fx = fx + w * s.mfx[j / S2];
+                fy = fy + w * s.mfy[j / S2];
+            }
+            R cx = s.upx[i] + fx * s.half_inv[i];
+            R cy = s.upy[i] + fy * s.half_inv[i];
             if (a.clamp) {
                 cx = ibm_clamp(cx);
                 cy = ibm_clamp(cy);
             }
-            upx[i] = cx;
-            upy[i] = cy;
-            ftx[i] = ftx[i] + fix[i];
-            fty[i] = fty[i] + fiy[i];
+            s.upx[i] = cx;
+            s.upy[i] = cy;
+            const R tx = s.ftx[i] + fx, ty = s.fty[i] + fy;
+            s.ftx[i] = tx;
+            s.fty[i] = ty;
+            if (last) {
+                const long long off = a.patch_nodes[i];
+                a.ibm_force[off] = tx;
+                a.ibm_force[a.plane + off] = ty;
+            }
         }
         __syncthreads();
     }
-    for (int i = tid; i < np; i += blockDim.x) {
-        const long long off = a.patch_nodes[i];
-        a.ibm_force[off] = ftx[i];
-        a.ibm_force[a.plane + off] = fty[i];
-    }
-    for (int k = tid; k < nm; k += blockDim.x) {
-        a.marker_force[k] = mtx[k];
-        a.marker_force[nm + k] = mty[k];
-    }
 }
 
-// the rounds for the stencil of a (2x2 or 4x4 nodes per marker)
+template <typename R>
+__device__ void ibm_iterate(const IbmData<R>& a, const IbmSmem<R>& s) {
+    if (a.stencil == 4) ibm_iterate_s<R, 16>(a, s);
+    else ibm_iterate_s<R, 4>(a, s);
+}
+
+// All rounds of one step with the patch read from a.patch_rho / a.patch_u;
+// sm holds ibm_smem_bytes_of<R> bytes.
 template <typename R>
 __device__ void ibm_rounds(const IbmData<R>& a, R* sm) {
-    if (a.stencil == 4) ibm_rounds_s<R, 16>(a, sm);
-    else ibm_rounds_s<R, 4>(a, sm);
+    const IbmSmem<R> s = ibm_layout(a, sm);
+    ibm_stage(a, s);
+    for (int i = threadIdx.x; i < a.npatch; i += blockDim.x)
+        ibm_set_patch(s, i, a.patch_rho[i], a.patch_u[i], a.patch_u[a.npatch + i]);
+    __syncthreads();
+    ibm_iterate(a, s);
 }
 
 }  // namespace lbmx

@@ -120,6 +120,7 @@ struct IbmData {
     int nm, npatch, iters, stencil;     // stencil: 2 or 4 nodes per axis
     const int* sten_idx;                // [nm][stencil^2] patch index or -1
     const float* sten_w;                // [nm][stencil^2] kernel weight
+    const int* spread;                  // [npatch + 1] offsets, then the stencil points of each patch node (ascending)
     const int* patch_nodes;             // [npatch] node offset (y*pitch + x)
     const R* patch_rho;                 // [npatch]
     const R* patch_u;                   // [2][npatch] uncorrected velocity
@@ -134,7 +135,7 @@ struct IbmData {
 using IbmArgs = IbmData<float>;
 // the IBM of one step: patch gather and marker rounds (lbmx_kernels.cuh)
 template <typename T>
-cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, float* patch_rho, float* patch_u, cudaStream_t s);
+cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, cudaStream_t s);
 
 // Many lattices in one persistent launch (lbmx_batch.cu).  Work items are
 // interior tiles and chunks of special units of every lattice; the

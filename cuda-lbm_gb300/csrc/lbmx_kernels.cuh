@@ -748,15 +748,18 @@ __global__ void get_populations_kernel(const StepArgs a, float* out, int last_pa
 
 // The IBM of one step in one CTA: density and uncorrected velocity of the
 // patch nodes (the reference interpolates from d_rho and the copy of d_u
-// taken before the force correction, IBMManager.cuh:227-228), then the
-// multi-direct rounds (ibm_rounds, lbmx_ibm.cuh).  Launched with programmatic
-// stream serialization like the step kernel: it waits for the previous step
-// before reading the populations and lets the next step kernel launch and
-// wait behind it.
+// taken before the force correction, IBMManager.cuh:227-228), gathered
+// straight into shared memory, then the multi-direct rounds (ibm_iterate,
+// lbmx_ibm.cuh).  The stencils and spread lists do not depend on the flow, so
+// they are staged before the wait for the previous step.  Launched with
+// programmatic stream serialization like the step kernel: it waits for the
+// previous step before reading the populations and lets the next step kernel
+// launch and wait behind it.
 template <typename T>
-__global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a, const IbmArgs ib, float* prho,
-                                                               float* pu) {
+__global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a, const IbmArgs ib) {
     extern __shared__ float sm[];
+    const IbmSmem<float> s = ibm_layout(ib, sm);
+    ibm_stage(ib, s);
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" :::);
     for (int i = threadIdx.x; i < ib.npatch; i += blockDim.x) {
@@ -773,12 +776,10 @@ __global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a,
             jy += (float)CY(q) * f[q];
         }
         const float inv = 1.0f / rho;
-        prho[i] = rho;
-        pu[i] = jx * inv;
-        pu[ib.npatch + i] = jy * inv;
+        ibm_set_patch(s, i, rho, jx * inv, jy * inv);
     }
     __syncthreads();
-    ibm_rounds<float>(ib, reinterpret_cast<float*>(sm));
+    ibm_iterate(ib, s);
 }
 
 template <typename T, int OP, int P, int MODE>
@@ -863,7 +864,7 @@ cudaError_t launch_get_populations(const StepArgs& a, float* out, cudaStream_t s
 }
 
 template <typename T>
-cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, float* prho, float* pu, cudaStream_t s) {
+cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, cudaStream_t s) {
     if (ib.npatch <= 0) return cudaSuccess;
     const size_t smem = ibm_smem_bytes_of<float>(ib.npatch, ib.nm, ib.stencil);
     // the attribute grows with the patch: raise it when a larger one comes
@@ -886,7 +887,7 @@ cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, float* prho, f
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, ibm_step_kernel<T>, a, ib, prho, pu);
+    return cudaLaunchKernelEx(&cfg, ibm_step_kernel<T>, a, ib);
 }
 
 #define LBMX_INSTANTIATE(T)                                                                              \
@@ -895,6 +896,6 @@ cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, float* prho, f
     template cudaError_t launch_edge_prepass<T>(const StepArgs&, float*, cudaStream_t);                  \
     template cudaError_t launch_init<T>(const StepArgs&, const float*, const float*, cudaStream_t);      \
     template cudaError_t launch_get_populations<T>(const StepArgs&, float*, cudaStream_t);               \
-    template cudaError_t launch_ibm_step<T>(const StepArgs&, const IbmArgs&, float*, float*, cudaStream_t);
+    template cudaError_t launch_ibm_step<T>(const StepArgs&, const IbmArgs&, cudaStream_t);
 
 }  // namespace lbmx

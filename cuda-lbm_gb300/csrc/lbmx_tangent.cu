@@ -248,6 +248,7 @@ struct lbmx_tangent {
     int nm = 0, npatch = 0, stencil = 0;
     int* patch_nodes = nullptr;
     int* sten_idx = nullptr;
+    int* spread = nullptr;
     float* sten_w = nullptr;
     D* patch_rho = nullptr;
     D* patch_u = nullptr;
@@ -284,10 +285,10 @@ dim3 node_grid(const lbmx_tangent* t) {
 }
 
 void free_markers(lbmx_tangent* t) {
-    cudaFree(t->patch_nodes); cudaFree(t->sten_idx); cudaFree(t->sten_w); cudaFree(t->patch_rho);
+    cudaFree(t->patch_nodes); cudaFree(t->sten_idx); cudaFree(t->sten_w); cudaFree(t->spread); cudaFree(t->patch_rho);
     cudaFree(t->patch_u); cudaFree(t->marker_u); cudaFree(t->marker_rho); cudaFree(t->marker_force);
     cudaFree(t->ibm_force);
-    t->patch_nodes = t->sten_idx = nullptr;
+    t->patch_nodes = t->sten_idx = t->spread = nullptr;
     t->sten_w = nullptr;
     t->patch_rho = t->patch_u = t->marker_u = t->marker_rho = t->marker_force = t->ibm_force = nullptr;
     t->nm = t->npatch = t->stencil = 0;
@@ -449,6 +450,9 @@ lbmx_status lbmx_tangent_set_markers(lbmx_tangent* t, const float* xy, int32_t n
     TAN_CUDA(t, cudaMemcpy(t->patch_nodes, nodes.data(), np * sizeof(int), cudaMemcpyHostToDevice));
     TAN_CUDA(t, cudaMemcpy(t->sten_idx, sidx.data(), sidx.size() * sizeof(int), cudaMemcpyHostToDevice));
     TAN_CUDA(t, cudaMemcpy(t->sten_w, sw.data(), sw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    const std::vector<int> spread = ibm_build_spread(np, sidx);
+    TAN_CUDA(t, cudaMalloc((void**)&t->spread, spread.size() * sizeof(int)));
+    TAN_CUDA(t, cudaMemcpy(t->spread, spread.data(), spread.size() * sizeof(int), cudaMemcpyHostToDevice));
     TAN_CUDA(t, cudaMemset(t->ibm_force, 0, 2 * (size_t)t->n * sizeof(D)));
     TAN_CUDA(t, cudaMemset(t->marker_force, 0, 2 * (size_t)n * sizeof(D)));
     TAN_CUDA(t, cudaFuncSetAttribute(tan_ibm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -478,6 +482,7 @@ lbmx_status lbmx_tangent_run(lbmx_tangent* t, int32_t nsteps, double* series) {
     ia.stencil = t->stencil;
     ia.sten_idx = t->sten_idx;
     ia.sten_w = t->sten_w;
+    ia.spread = t->spread;
     ia.patch_nodes = t->patch_nodes;
     ia.patch_rho = t->patch_rho;
     ia.patch_u = t->patch_u;

@@ -171,6 +171,25 @@ def test_channel_ibm_cylinder(quirks):
     assert np.allclose(dl, -Fo.sum(axis=1), atol=1e-4)
 
 
+@pytest.mark.parametrize("storage", [0, 1])
+@pytest.mark.parametrize("stencil_quirks", [0, C.QUIRKS_REFERENCE])
+def test_ibm_is_bitwise_reproducible(storage, stencil_quirks):
+    """The spread adds each node's stencil contributions in a fixed order, so
+    two runs of the same IBM channel agree bit for bit: populations, marker
+    forces and drag/lift."""
+    mk = C.cylinder_markers(32.3, 24.1, 6.0, 32)
+    c = C.channel(96, 48, quirks=stencil_quirks, markers=mk, u_in=0.05)
+    runs = []
+    for _ in range(2):
+        L = C.make_lattice(c, storage=storage)
+        L.step(200)
+        F, dl = L.marker_forces()
+        runs.append((np.nan_to_num(L.populations()), F, np.asarray(dl)))
+    (pa, Fa, da), (pb, Fb, db) = runs
+    assert np.array_equal(pa, pb)
+    assert np.array_equal(Fa, Fb) and np.array_equal(da, db)
+
+
 def test_poiseuille_ibm_reference_scenario():
     # PoiseuilleScenario::add_bodies: cylinder of D=16 at (48, NY/2), 16 markers
     mk = C.cylinder_markers(48.0, 50.0, 8.0, 16)
