@@ -11,6 +11,9 @@
 #   ref_build.sh timers    compile oracle/ref_timer.cu the same way, one binary
 #                          per timed configuration (oracle/_ref/bin/time_*), to
 #                          time the reference's own GPU step
+#   ref_build.sh validators  compile oracle/ref_validate.cu the same way, once per
+#                          unchanged 2-D scenario header (oracle/_ref/bin/validate_*),
+#                          to record the scenarios' own compute_error
 #
 # oracle/_ref/ is git-ignored; it travels with the working tree, so `build`
 # also works where the reference checkout is absent.  The patches are the
@@ -23,6 +26,8 @@
 #                          (u[2*node], get_node_index(node)+q)
 #   lbm.cuh:35             `private:` -> `public:` so the harness can read d_f
 #   adapters.cuh:101       silence the per-node OptimalAdapter printf
+#   flowPastCylinderScenario.cuh:12  `BGK` -> `BGK<2>` (the header names the
+#                          template without its argument and builds nowhere as shipped)
 set -euo pipefail
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${LBMX_REFERENCE:-/root/reference}
@@ -60,6 +65,8 @@ EOF
     sed -i '35s/^private:/public:/' "$S/core/lbm.cuh"
     sed -i '101s/if (fabsf(tau_star_old) > 0.5f || fabsf(tau_star_old) < 0.1f){/if (false) {/' \
         "$S/core/collision/adapters.cuh"
+    sed -i -E 's/^([[:space:]]*)BGK(\r?)$/\1BGK<2>\2/' "$S/scenarios/flowPastCylinder/flowPastCylinderScenario.cuh"
+    grep -q 'BGK<2>' "$S/scenarios/flowPastCylinder/flowPastCylinderScenario.cuh"
     grep -q 'float\* rho, int\* boundary_flags' "$S/core/boundaries/boundaries.cuh"
     grep -q '^// #define SOA' "$S/core/lbm_constants.cuh"
     grep -q '^public:' "$S/core/lbm.cuh"
@@ -87,6 +94,16 @@ TIMERS=(
   "time_tg256_bgk|-DNX=256 -DNY=256 -DPERIODIC_X -DPERIODIC_Y -DLBX_CASE=1 -DLBX_OPID=0 -DLBX_NU=0.01f"
 )
 
+# unchanged scenario headers | struct | their as-shipped lattice and periodicity
+# (src/defines.hpp:20-35; periodic where the flow is: Taylor-Green in x and y,
+# the Poiseuille channel in x)
+VALIDATORS=(
+  "validate_tg|scenarios/taylorGreen/taylorGreenScenario.cuh|TaylorGreenScenario|-DNX=256 -DNY=256 -DSCALE=2 -DPERIODIC_X -DPERIODIC_Y"
+  "validate_ldc|scenarios/lidDrivenCavity/lidDrivenCavityScenario.cuh|LidDrivenScenario|-DNX=129 -DNY=129"
+  "validate_poiseuille|scenarios/poiseuille/poiseuilleScenario.cuh|PoiseuilleScenario|-DNX=150 -DNY=100 -DPERIODIC_X"
+  "validate_cylinder|scenarios/flowPastCylinder/flowPastCylinderScenario.cuh|FlowPastCylinderScenario|-DNX=256 -DNY=128 -DLBX_DEFINE_CURRENT_VELOCITY"
+)
+
 build() {
     local S=$OUT/src
     [ -d "$S" ] || { echo "no patched sources in $OUT/src (run: ref_build.sh sources)"; exit 1; }
@@ -99,6 +116,14 @@ $S/IBM/IBM_impl.cu $S/IBM/IBM_generators.cu $S/util/utility.cu"
     local driver=$HERE/ref_harness.cu
     local list=("${CASES[@]}")
     if [ "${1:-}" = timers ]; then driver=$HERE/ref_timer.cu; list=("${TIMERS[@]}"); fi
+    if [ "${1:-}" = validators ]; then
+        driver=$HERE/ref_validate.cu
+        list=()
+        for v in "${VALIDATORS[@]}"; do
+            IFS='|' read -r vn vh vs vd <<< "$v"
+            list+=("$vn|-DLBX_SCENARIO_HEADER=\"$vh\" -DLBX_SCENARIO=$vs $vd")
+        done
+    fi
     for c in "${list[@]}"; do
         local name=${c%%|*} defs=${c#*|}
         ( $NVCC $FLAGS $defs "$driver" $SRCS -o "$OUT/bin/$name" > "$OUT/obj/$name.log" 2>&1 \
@@ -112,11 +137,14 @@ $S/IBM/IBM_impl.cu $S/IBM/IBM_generators.cu $S/util/utility.cu"
 }
 
 list() { for c in "${CASES[@]}"; do echo "${c%%|*}|${c#*|}"; done; }
+validators_list() { for v in "${VALIDATORS[@]}"; do echo "$v"; done; }
 
 case "${1:-}" in
     sources) sources ;;
     build) build ;;
     timers) build timers ;;
+    validators) build validators ;;
     list) list ;;
-    *) echo "usage: $0 sources|build|timers|list"; exit 2 ;;
+    validators-list) validators_list ;;
+    *) echo "usage: $0 sources|build|timers|validators|list|validators-list"; exit 2 ;;
 esac

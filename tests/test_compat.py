@@ -10,6 +10,14 @@
 * GPU: the golden scenarios (oracle/ref_scenarios.cuh) -- the very source the
   reference's build ran to write tests/golden/ -- run on lbmx through
   lbmx_compat::create and reproduce the reference's dumps.
+* GPU: the reference's four 2-D scenario headers themselves run on lbmx
+  (tests/compat/scenario_runner.cu) to the steps where its main loop
+  validates; their own compute_error, evaluated on the lbmx solver, and the
+  velocity field it read match what the reference's build reported for the
+  same headers (tests/golden/ref_validation.npz, made by
+  tests/golden/make_ref_validation.py).  The headers are read from the
+  copy under oracle/_ref/src (written by `oracle/ref_build.sh sources`);
+  the test skips where that copy is absent.
 """
 import ctypes
 import glob
@@ -23,7 +31,10 @@ import pytest
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 COMPAT = os.path.join(REPO, "cuda-lbm_gb300", "compat")
 INCLUDE = os.path.join(REPO, "include")
-REF_SCEN = "/root/reference/src/scenarios"
+# the reference checkout (LBMX_REFERENCE, as oracle/ref_build.sh resolves it)
+REF_SCEN = os.path.join(os.environ.get("LBMX_REFERENCE", "/root/reference"), "src", "scenarios")
+# the recipe's copy of the reference sources, which travels with the tree
+REF_COPY = os.path.join(REPO, "oracle", "_ref", "src")
 BUILD = os.path.join(REPO, "tests", "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -115,3 +126,85 @@ def test_golden_scenario_runs_unchanged_on_lbmx(name):
         assert np.abs(f[k][m] - z["f_%d" % t][m]).max() <= 2e-5
         assert np.abs(rho[k] - z["rho_%d" % t]).max() <= 2e-5
         assert np.abs(u[k] - z["u_%d" % t]).max() <= 2e-5
+
+
+def _validators():
+    out = subprocess.check_output(["bash", os.path.join(REPO, "oracle", "ref_build.sh"), "validators-list"], text=True)
+    return [dict(zip(("name", "header", "struct", "defs"), ln.split("|"))) for ln in out.splitlines()]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SCEN) or not os.path.isdir(REF_COPY),
+                    reason="reference checkout or its copy not present")
+@pytest.mark.parametrize("name", ["validate_tg", "validate_ldc", "validate_poiseuille"])
+def test_copied_scenario_headers_are_the_reference_files(name):
+    """The validator tests run the copy under oracle/_ref/src; for these three
+    scenarios the copy, with its functors header, is the checkout's file byte
+    for byte (only the cylinder header gets its one-token fix)."""
+    v = {x["name"]: x for x in _validators()}[name]
+    d = os.path.dirname(v["header"])
+    src = os.path.join(REF_SCEN, os.path.relpath(d, "scenarios"))
+    for f in sorted(x for x in os.listdir(src) if os.path.isfile(os.path.join(src, x))):
+        a = open(os.path.join(src, f), "rb").read()
+        b = open(os.path.join(REF_COPY, d, f), "rb").read()
+        assert a == b, f
+
+
+def _build_validation_runner(v):
+    import build as B
+    lib = B.build()
+    os.makedirs(BUILD, exist_ok=True)
+    so = os.path.join(BUILD, "scenario_%s.so" % v["name"])
+    header = os.path.join(REF_COPY, v["header"])
+    cmd = ["nvcc"] + ARCH + ["-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-w", "-I" + COMPAT, "-I" + INCLUDE,
+                             '-DLBX_SCENARIO_HEADER="%s"' % header, "-DLBX_SCENARIO=" + v["struct"]] + \
+        v["defs"].split() + [os.path.join(REPO, "tests", "compat", "scenario_runner.cu"), "-L" + os.path.dirname(lib),
+                             "-llbmx", "-Xlinker", "-rpath," + os.path.dirname(lib), "-o", so]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return so
+
+
+# |compute_error(lbmx) - compute_error(reference)| in the validators' own
+# unit (percent), and max |du| over the probed nodes, per scenario.  The
+# Poiseuille channel carries the reference's float-atomic IBM, which is not
+# reproducible run to run.  Taylor-Green's error against its analytic field
+# is only 0.03-0.24 %, the size of FP32 rounding in either implementation;
+# there the validator's difference is held to what the velocity difference
+# explains: compute_error is 100 |u - a| / |a|, so by the triangle inequality
+# |e1 - e2| <= 100 |u1 - u2| / |a|, with |a| ~ |u_ref| and the norms
+# estimated on the probe (three times that, for the sampling).
+VALIDATION_TOL = {"validate_tg": ("velocity", 3e-6), "validate_ldc": (1e-2, 2e-5),
+                  "validate_poiseuille": (5e-2, 2e-5), "validate_cylinder": (None, 2e-5)}
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.path.isdir(REF_COPY), reason="no copy of the reference sources under oracle/_ref/src")
+@pytest.mark.parametrize("name", ["validate_tg", "validate_ldc", "validate_poiseuille", "validate_cylinder"])
+def test_reference_scenario_validators_on_lbmx(name):
+    z = np.load(os.path.join(REPO, "tests", "golden", "ref_validation.npz"))
+    meta = json.loads(str(z["meta"]))
+    steps, stride = meta["steps"], meta["probe_stride"]
+    v = {x["name"]: x for x in _validators()}[name]
+    lib = ctypes.CDLL(_build_validation_runner(v))
+    nx, ny = ctypes.c_int(), ctypes.c_int()
+    lib.scenario_lattice(ctypes.byref(nx), ctypes.byref(ny))
+    err = np.zeros(len(steps), np.float32)
+    u = np.zeros((len(steps), ny.value, nx.value, 2), np.float32)
+    arr = (ctypes.c_int * len(steps))(*steps)
+    rc = lib.run_validation(arr, len(steps), ctypes.c_void_p(err.ctypes.data), ctypes.c_void_p(u.ctypes.data))
+    assert rc == 0
+    ref_err, ref_u = z[name + "_err"], z[name + "_u"]
+    etol, utol = VALIDATION_TOL[name]
+    for k, t in enumerate(steps):
+        du = float(np.abs(u[k, ::stride, ::stride, :] - ref_u[k]).max())
+        de = abs(float(err[k]) - float(ref_err[k]))
+        print("%s t=%d compute_error lbmx %.6g reference %.6g | max|du| %.3g" % (name, t, err[k], ref_err[k], du))
+        assert du <= utol, (t, du)
+        if etol is None:
+            assert err[k] == ref_err[k]  # the cylinder's validator returns -1
+            continue
+        tol = etol
+        if etol == "velocity":
+            d = u[k, ::stride, ::stride, :] - ref_u[k]
+            tol = 3 * 100 * np.sqrt((d.astype(np.float64) ** 2).sum() / (ref_u[k].astype(np.float64) ** 2).sum()) + 1e-3
+        assert de <= tol, (t, float(err[k]), float(ref_err[k]), tol)
