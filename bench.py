@@ -32,7 +32,9 @@ half-way moving wall, half-way bounce-back on the other walls, Re = 1000
             against FP64 central differences of the oracle.
   validation  the Taylor-Green vortex (256^2, 2000 steps) against its
             analytic decay, and the IBM cylinder channel (2048 x 512, Re 100)
-            with its MLUPS, drag and lift in FP32 and FP16 offset storage.
+            run 200k steps from rest in FP32 and FP16 offset storage: MLUPS,
+            mean C_D, C_L amplitude and Strouhal number of the shedding state
+            from every step's drag and lift.
   cpu_baseline  the FP64 CPU oracle (OpenMP, all host cores) on the same
             workload, 200 steps.
 
@@ -326,13 +328,9 @@ def bench_validation(args, torch, stream, device):
 
     Taylor-Green vortex: 256 x 256, fully periodic, BGK, nu 0.01, u0 0.04,
     2000 steps, velocity amplitude against exp(-2 nu k^2 t) (the lattice,
-    4.7 MB, stays in L2).  Flow past a cylinder: 2048 x 512, Zou-He
-    parabolic inlet (peak 0.05), Zou-He pressure outlet, bounce-back walls,
-    cylinder D = 64 at (256, 256) as 256 IBM markers (multi-direct forcing,
-    4-point Peskin kernel), Re 100 on D and the peak inlet velocity, FP32 and
-    FP16 offset storage: MLUPS with the IBM kernels in the step, and drag and
-    lift after `args.cyl_steps` steps (the start of the run, not the
-    shedding state)."""
+    4.7 MB, stays in L2).  Flow past a cylinder: the shedding run of
+    bench_cylinder_shedding, then the drag sensitivity of the same
+    configuration."""
     import cases as C
     import lbmx
 
@@ -367,27 +365,86 @@ def bench_validation(args, torch, stream, device):
                            "amplitude": amp, "analytic": exact, "rel_err": abs(amp - exact) / exact,
                            "MLUPS": round(n * n * T / (ms * 1e-3) / 1e6, 1)}
     del L
-    nx, ny, D, U = 2048, 512, 64, 0.05
+    out["cylinder_shedding"] = bench_cylinder_shedding(args, torch, stream, device, lattice)
+    out["drag_sensitivity"] = bench_drag_sensitivity(args, torch, stream, device)
+    return out
+
+
+def shedding_stats(series, q, D, U):
+    """Mean C_D, C_L amplitude and Strouhal number of the last half of a
+    {drag, lift} series.  The period is the mean spacing of the upward zero
+    crossings of C_L - mean (linear interpolation between steps); the run
+    counts as periodic when the C_L amplitude of the last quarter is within 5%
+    of the third quarter's."""
+    T = series.shape[0]
+    cd = series[:, 0] / q
+    cl = series[:, 1] / q
+    h = cd[T // 2:], cl[T // 2:]
+    cl_c = h[1] - h[1].mean()
+    up = np.nonzero((cl_c[:-1] < 0) & (cl_c[1:] >= 0))[0]
+    crossings = up + cl_c[up] / (cl_c[up] - cl_c[up + 1])
+    st = None
+    if len(crossings) >= 3:
+        period = float(np.mean(np.diff(crossings)))
+        st = D / (period * U)
+    q3 = cl[T // 2: 3 * T // 4]
+    q4 = cl[3 * T // 4:]
+    a3, a4 = 0.5 * float(q3.max() - q3.min()), 0.5 * float(q4.max() - q4.min())
+    onset = None
+    if a4 > 0:
+        big = np.nonzero(np.abs(cl - cl[T // 2:].mean()) > 0.1 * a4)[0]
+        onset = int(big[0]) + 1 if len(big) else None
+    return {"C_D_mean": float(h[0].mean()), "C_D_amplitude": 0.5 * float(h[0].max() - h[0].min()),
+            "C_L_amplitude": a4, "C_L_mean": float(h[1].mean()), "strouhal": st,
+            "shedding_periods_in_last_half": int(len(crossings)), "periodic": bool(a4 > 0 and abs(a4 - a3) <= 0.05 * a4),
+            "onset_step": onset}
+
+
+def bench_cylinder_shedding(args, torch, stream, device, lattice):
+    """Flow past a cylinder (the C4 configuration): 2048 x 512, Zou-He
+    parabolic inlet (peak U = 0.05), Zou-He pressure outlet, bounce-back walls,
+    cylinder D = 64 at (256, 256) (half a node above the channel's centre
+    line) as 256 IBM markers (multi-direct forcing, 4-point Peskin kernel), Re
+    100 on D and U, BGK, from rest for `args.cyl_steps` steps in FP32 and FP16
+    offset storage.  Every step's drag and lift are recorded by the IBM kernel
+    itself (lbmx_step_forces into pinned host memory); C_D, C_L = force / (1/2
+    rho U^2 D) with rho = 1; Strouhal = f D / U.  MLUPS over the whole run."""
+    import cases as C
+
+    nx, ny, D, U, T = 2048, 512, 64, 0.05, args.cyl_steps
     markers = C.cylinder_markers(256, 256, D / 2, 256)
-    cyl = {}
+    q = 0.5 * 1.0 * U * U * D
+    res = {}
     for storage in (0, 1):
         c = C.channel(nx, ny, op=C.BGK, nu=U * D / 100.0, u_in=U, inlet="parabolic", outlet="zouhe_p",
                       markers=markers)
         L = lattice(c, storage)
-        L.step(10)
-        ms = timed(L, args.cyl_steps)
-        _, dl = L.marker_forces()
-        q = 0.5 * 1.0 * U * U * D
-        cyl[STORAGE_NAME[storage]] = {"MLUPS": round(nx * ny * args.cyl_steps / (ms * 1e-3) / 1e6, 1),
-                                      "drag": float(dl[0]), "lift": float(dl[1]),
-                                      "C_D": float(dl[0]) / q, "C_L": float(dl[1]) / q}
+        series = torch.zeros(2 * T, dtype=torch.float64).pin_memory()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.step_forces(T, out=series)
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1)
+        sr = series.numpy().reshape(T, 2).copy()
+        st = shedding_stats(sr, q, D, U)
+        st["MLUPS"] = round(nx * ny * T / (ms * 1e-3) / 1e6, 1)
+        st["us_per_step"] = round(ms * 1e3 / T, 2)
+        st["finite"] = bool(np.isfinite(sr).all())
+        res[STORAGE_NAME[storage]] = st
         del L
-    cyl["f16_drag_rel_diff"] = abs(cyl["f16_offset"]["drag"] - cyl["f32"]["drag"]) / abs(cyl["f32"]["drag"])
-    cyl["workload"] = ("cylinder 2048x512, D 64 at (256,256), 256 IBM markers, BGK, Re 100, Zou-He parabolic inlet "
-                       "0.05, Zou-He pressure outlet, %d steps after 10" % args.cyl_steps)
-    out["cylinder"] = cyl
-    out["drag_sensitivity"] = bench_drag_sensitivity(args, torch, stream, device)
-    return out
+
+    def rel(k):
+        a, b = res["f16_offset"][k], res["f32"][k]
+        return None if a is None or b is None or b == 0 else abs(a - b) / abs(b)
+
+    res["f16_vs_f32"] = {"C_D_mean_rel_diff": rel("C_D_mean"), "C_L_amplitude_rel_diff": rel("C_L_amplitude"),
+                         "strouhal_rel_diff": rel("strouhal")}
+    res["workload"] = ("cylinder 2048x512, D 64 at (256,256), 256 IBM markers, BGK, Re 100 on D and the peak inlet "
+                       "velocity 0.05, Zou-He parabolic inlet, Zou-He pressure outlet, %d steps from rest; statistics "
+                       "over the last half" % T)
+    res["steps"] = T
+    return res
 
 
 def bench_drag_sensitivity(args, torch, stream, device):
@@ -400,7 +457,7 @@ def bench_drag_sensitivity(args, torch, stream, device):
     import cases as C
     import lbmx
 
-    nx, ny, D, U, T = 2048, 512, 64, 0.05, args.cyl_steps
+    nx, ny, D, U, T = 2048, 512, 64, 0.05, args.sens_steps
     half = T // 2
     mk = C.cylinder_markers(256, 256, D / 2, 256)
 
@@ -428,11 +485,7 @@ def bench_drag_sensitivity(args, torch, stream, device):
         L.init(np.ones((ny, nx), np.float32), np.zeros((2, ny, nx), np.float32))
         L.set_markers(mk)
         L.step(half)
-        d = []
-        for _ in range(T - half):
-            L.step(1)
-            d.append(L.marker_forces()[1][0])
-        return float(np.mean(d))
+        return float(L.step_forces(T - half)[:, 0].mean())
 
     h = 0.01 * U
     fd = (engine_mean_drag(U + h) - engine_mean_drag(U - h)) / (2 * h)
@@ -569,6 +622,66 @@ def bench_adjoint(args, torch, stream, device):
     return out
 
 
+def bench_config(n, world):
+    """The config dict of the headline workload, shared by both arms."""
+    return {"workload": "lid-driven cavity %dx%d, D2Q9 MRT, lid 0.1 half-way moving wall, Re 1000" % (n, n),
+            "nodes": n * n,
+            "l2": "GPU arm: flushed before every timed step (256 MB write, then 256 MB read of a second buffer); "
+                  "CPU arm: FP64 populations (%d MB) stream from DRAM" % (2 * 9 * 8 * n * n // 2 ** 20),
+            "parallelism": "replica per GPU" if world > 1 else "single GPU"}
+
+
+def bench_reference_gpu(args, torch, stream, device):
+    """The reference's own CUDA step on this GPU, beside lbmx on the same
+    configuration: the 1024^2 MRT lid-driven cavity with the reference's
+    regularized walls and lid (nu 0.1024, Re 1000) and the 256^2 BGK
+    Taylor-Green vortex, both run back to back (no L2 flush), CUDA events
+    over 1000 steps after 50 warm-up steps on each side.  The reference
+    binaries are built by oracle/ref_build.sh timers (from the recipe's copy
+    of the reference sources) and run the call sequence of its main loop
+    (src/main.cu:96-114)."""
+    import cases as C
+    import lbmx
+
+    out = {}
+    cfgs = {"cavity1024_mrt": C.cavity_regularized(1024, 1024, op=C.MRT, nu=0.1024, u_lid=0.1,
+                                                   quirks=C.QUIRKS_REFERENCE),
+            "tg256_bgk": C.taylor_green(256, 256, op=C.BGK, nu=0.01, u0=0.04, quirks=C.QUIRKS_REFERENCE)}
+    for name, c in cfgs.items():
+        exe = os.path.join(REPO, "oracle", "_ref", "bin", "time_" + name)
+        if not os.path.exists(exe):
+            out[name] = {"unavailable": "reference timer binary not built (oracle/ref_build.sh timers)"}
+            continue
+        r = subprocess.run([exe, "50", "1000"], capture_output=True, text=True, timeout=300)
+        if r.returncode != 0:
+            out[name] = {"unavailable": "reference timer exited %d: %s" % (r.returncode, r.stderr.strip()[-200:])}
+            continue
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith('{"nx"')]
+        if not lines:
+            out[name] = {"unavailable": "reference timer printed no timing line"}
+            continue
+        ref = json.loads(lines[-1])
+        L = lbmx.Lattice(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], periodic=c["periodic"],
+                         quirks=c["quirks"], u_bc=c["u_bc"], device=device, stream=stream.cuda_stream)
+        L.set_flags(c["flags"])
+        L.init(np.asarray(c["rho"], np.float32), np.asarray(c["u"], np.float32))
+        L.step(50, 0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.step(1000, 0)
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / 1000
+        del L
+        nodes = c["nx"] * c["ny"]
+        out[name] = {"reference_ms_per_step": ref["ms_per_step"], "reference_MLUPS": ref["mlups"],
+                     "lbmx_ms_per_step": round(ms, 5), "lbmx_MLUPS": round(nodes / (ms * 1e3), 1),
+                     "lbmx_over_reference": round(ref["ms_per_step"] / ms, 1)}
+    out["how"] = ("back-to-back steps, CUDA events over 1000 steps after 50 warm-up steps; the reference binaries "
+                  "run its LBM<2> main-loop call sequence on the default stream; lbmx with the reference's quirks on")
+    return out
+
+
 def bench_reference(args, rank, world):
     """CPU implementation of the reference step (the oracle port), all host threads."""
     if rank != 0:
@@ -590,10 +703,10 @@ def bench_reference(args, rank, world):
     mlups = n * n * per_step / t / 1e6
     line = {
         "impl": "reference", "metric": metric_name(n), "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3 / per_step, 4),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 4),
+        "lbm_steps_per_bench_step": per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "lid-driven cavity %dx%d MRT, lid 0.1, Re 1000" % (n, n), "nodes": n * n,
-                   "lbm_steps_per_bench_step": per_step},
+        "config": bench_config(n, world),
         "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
                          "sample": "%d bench steps x %d LBM steps of the %dx%d cavity" % (args.steps, per_step, n, n)},
         "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -615,7 +728,8 @@ def main():
     ap.add_argument("--ens-steps", type=int, default=64)
     ap.add_argument("--ens-err-count", type=int, default=6)
     ap.add_argument("--ens-err-steps", type=int, default=1000)
-    ap.add_argument("--cyl-steps", type=int, default=2000)
+    ap.add_argument("--cyl-steps", type=int, default=200000, help="steps of the cylinder shedding run")
+    ap.add_argument("--sens-steps", type=int, default=2000, help="steps of the drag-sensitivity run")
     ap.add_argument("--steady-steps", type=int, default=100000)
     ap.add_argument("--steady-fp64", action="store_true",
                     help="also run the 256^2 cavity to steady state against the FP64 oracle (about a minute of CPU)")
@@ -678,9 +792,7 @@ def main():
         "metric": metric_name(n, main_storage), "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "lid-driven cavity %dx%d, D2Q9 MRT, lid 0.1 half-way moving wall, Re 1000" % (n, n),
-                   "nodes": nodes, "storage": STORAGE_NAME[main_storage], "l2": "flushed before every timed step: 256 MB write, then 256 MB read of a second buffer",
-                   "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+        "config": bench_config(n, world), "storage": STORAGE_NAME[main_storage],
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": None,
                      "algorithmic_bytes_per_lu": BYTES_PER_LU[main_storage], "peak_kind": peak_kind + " burst (hbm_gbs)"},
@@ -779,6 +891,11 @@ def main():
         line["adjoint"] = bench_adjoint(args, torch, stream, local)
         # ---- Taylor-Green decay and the IBM cylinder
         line["validation"] = bench_validation(args, torch, stream, local)
+        # ---- the reference's own GPU step on this GPU, beside lbmx
+        try:
+            line["reference_gpu"] = bench_reference_gpu(args, torch, stream, local)
+        except Exception as exc:  # a measurement of the reference: never fails the bench
+            line["reference_gpu"] = {"unavailable": "%s: %s" % (type(exc).__name__, exc)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

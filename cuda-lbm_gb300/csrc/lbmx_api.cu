@@ -344,7 +344,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
     ALLOC(h->u_out, (size_t)2 * g.plane * sizeof(float));
     ALLOC(h->staging, (size_t)3 * n * sizeof(float));
     ALLOC(h->counter, sizeof(unsigned int));
-    ALLOC(h->sums, kNumSums * sizeof(double));
+    ALLOC(h->sums, kSumsBufferLen * sizeof(double));
     ALLOC(h->avg, 3 * sizeof(float));
     ALLOC(h->error_word, sizeof(unsigned int));
     ALLOC(h->tile_counter, 2 * sizeof(unsigned long long));
@@ -360,7 +360,7 @@ lbmx_status lbmx_create(const lbmx_params* p, lbmx_handle** out) {
         h->own_stream = true;
     }
     cudaMemsetAsync(h->counter, 0, sizeof(unsigned int), h->stream);
-    cudaMemsetAsync(h->sums, 0, kNumSums * sizeof(double), h->stream);
+    cudaMemsetAsync(h->sums, 0, kSumsBufferLen * sizeof(double), h->stream);
     cudaMemsetAsync(h->avg, 0, 3 * sizeof(float), h->stream);
     cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream);
     cudaMemsetAsync(h->tile_counter, 0, 2 * sizeof(unsigned long long), h->stream);
@@ -518,7 +518,7 @@ lbmx_status lbmx_init_from_fields(lbmx_handle* h, const float* rho, const float*
 // FP64 sums only; ke: the sums include the kinetic energy; series: where the
 // step's series entry (sums 0..2, then the kinetic energy) also goes.
 static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, bool ke,
-                            double* series = nullptr) {
+                            double* series = nullptr, double* force_series = nullptr) {
     const long long s = h->t + 1;
     StepArgs a = base_args(h);
     set_step(h, a, s);
@@ -548,6 +548,7 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, b
         ia.plane = h->g.plane;
         ia.clamp = (h->p.quirks & LBMX_QUIRK_IBM_CLAMP) ? 1 : 0;
         ia.ds = h->p.ibm_ds;
+        ia.force_series = force_series;
         LBMX_CUDA(h, dispatch(storage, [&](auto tag) {
                       return launch_ibm_step<decltype(tag)>(a, ia, st);
                   }));
@@ -669,6 +670,48 @@ lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, doubl
         LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
         LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
         if (w) return fail(h, LBMX_ERR_NONFINITE, "lbmx_step_sums: non-finite density at step %lld", h->t);
+    }
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_step_forces(lbmx_handle* h, int32_t nsteps, uint32_t flags, double* series) {
+    if (!h || !series) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step_forces: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_step_forces: call lbmx_init_from_fields first");
+    if (nsteps < 0) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step_forces: nsteps < 0");
+    if (h->nm <= 0) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_step_forces: the lattice has no IBM markers");
+    cudaSetDevice(h->p.device);
+    const bool check = (flags & LBMX_STEP_CHECK_FINITE) != 0;
+    if (check) LBMX_CUDA(h, cudaMemsetAsync(h->error_word, 0, sizeof(unsigned int), h->stream));
+    // as lbmx_step_sums: written by the kernel where it can reach the series,
+    // else through a device slot (the sums buffer's spare entries) per step
+    cudaPointerAttributes attr;
+    bool direct = false;
+    if (cudaPointerGetAttributes(&attr, series) == cudaSuccess)
+        direct = attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged ||
+                 (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr);
+    else
+        cudaGetLastError();
+    double* dev_series = direct ? static_cast<double*>(attr.devicePointer) : nullptr;
+    double* slot = h->sums + kSumForces;
+    const bool ke = (flags & LBMX_STEP_KINETIC_ENERGY) != 0;
+    for (int i = 0; i < nsteps; i++) {
+        const bool last = i == nsteps - 1;
+        lbmx_status st = run_step(h, last && (flags & LBMX_STEP_STORE_MOMENTS), last && check,
+                                  (flags & LBMX_STEP_SUMS) != 0, ke, nullptr,
+                                  direct ? dev_series + 2 * (size_t)i : slot);
+        if (st != LBMX_OK) return st;
+        if (!direct)
+            LBMX_CUDA(h, cudaMemcpyAsync(series + 2 * (size_t)i, slot, 2 * sizeof(double), cudaMemcpyDefault,
+                                         h->stream));
+    }
+    lbmx_status fs = flush_sums(h);
+    if (fs != LBMX_OK) return fs;
+    if (!direct || check) {
+        unsigned int w = 0;
+        if (check)
+            LBMX_CUDA(h, cudaMemcpyAsync(&w, h->error_word, sizeof(w), cudaMemcpyDeviceToHost, h->stream));
+        LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (w) return fail(h, LBMX_ERR_NONFINITE, "lbmx_step_forces: non-finite density at step %lld", h->t);
     }
     return LBMX_OK;
 }

@@ -128,6 +128,7 @@ struct IbmData {
     R* marker_rho;                      // [nm]
     R* marker_force;                    // [2][nm] summed over iterations
     R* ibm_force;                       // [2][plane] dense Eulerian force
+    double* force_series;               // this step's {drag, lift} entry or null (engine only)
     long long plane;
     int clamp;
     float ds;
@@ -172,6 +173,10 @@ constexpr int kNumSums = 6;
 constexpr int kSumKE = 3;
 constexpr int kSumSlots = 32;
 constexpr int kAccPerSet = kSumSlots * kNumSums;
+// the handle's sums buffer holds two more doubles after the sums: the
+// drag / lift slot lbmx_step_forces copies pageable series from
+constexpr int kSumForces = kNumSums;
+constexpr int kSumsBufferLen = kNumSums + 2;
 
 // Interior-path variant of a step launch:
 //   kModeLean  no per-node force or Brinkman field, no moment store, no sums,

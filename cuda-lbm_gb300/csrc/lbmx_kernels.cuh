@@ -780,6 +780,23 @@ __global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a,
     }
     __syncthreads();
     ibm_iterate(ib, s);
+    // drag and lift of the step: minus the summed marker forces, in FP64,
+    // each lane taking every 32nd marker, then a fixed shuffle tree
+    if (ib.force_series && threadIdx.x < 32) {
+        double dx = 0.0, dy = 0.0;
+        for (int k = threadIdx.x; k < ib.nm; k += 32) {
+            dx += (double)s.mtx[k];
+            dy += (double)s.mty[k];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            dx += __shfl_xor_sync(0xffffffffu, dx, o);
+            dy += __shfl_xor_sync(0xffffffffu, dy, o);
+        }
+        if (threadIdx.x == 0) {
+            ib.force_series[0] = -dx;
+            ib.force_series[1] = -dy;
+        }
+    }
 }
 
 template <typename T, int OP, int P, int MODE>

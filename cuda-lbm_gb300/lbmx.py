@@ -32,7 +32,7 @@ STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "INV
           5: "NOT_INITIALIZED", 6: "UNSUPPORTED", 7: "NONFINITE", 8: "TOO_LARGE"}
 
 EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy", "lbmx_set_flags",
-            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_moment_sums_async", "lbmx_step_sums", "lbmx_kinetic_energy",
+            "lbmx_init_from_fields", "lbmx_set_force_field", "lbmx_set_brinkman", "lbmx_step", "lbmx_step_ex", "lbmx_moments", "lbmx_moment_sums_async", "lbmx_step_sums", "lbmx_step_forces", "lbmx_kinetic_energy",
             "lbmx_get_populations", "lbmx_averages", "lbmx_ibm_set_markers", "lbmx_ibm_forces", "lbmx_time",
             "lbmx_synchronize", "lbmx_last_error", "lbmx_moment_sums_noalloc", "lbmx_checkpoint_save",
             "lbmx_checkpoint_load", "lbmx_write_vti", "lbmx_batch_create", "lbmx_batch_destroy",
@@ -98,6 +98,8 @@ def load_library(path=LIB_PATH):
     lib.lbmx_moment_sums_async.restype = ctypes.c_int32
     lib.lbmx_step_sums.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
     lib.lbmx_step_sums.restype = ctypes.c_int32
+    lib.lbmx_step_forces.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
+    lib.lbmx_step_forces.restype = ctypes.c_int32
     lib.lbmx_kinetic_energy.argtypes = [vp, vp]
     lib.lbmx_kinetic_energy.restype = ctypes.c_int32
     lib.lbmx_get_populations.argtypes = [vp, vp]
@@ -243,6 +245,18 @@ class Lattice:
 
     def step(self, n=1, flags=STEP_STORE_MOMENTS):
         self._check(self.lib.lbmx_step_ex(self.h, int(n), int(flags)))
+
+    def step_forces(self, n, flags=0, out=None):
+        """n steps recording each step's drag and lift (lbmx_step_forces):
+        an (n, 2) FP64 array.  `out` may be a pinned-host or CUDA torch
+        tensor of n*2 doubles, which the IBM kernel writes directly; then
+        the call returns without waiting and `out` is returned."""
+        if out is None:
+            res = np.zeros((int(n), 2), np.float64)
+            self._check(self.lib.lbmx_step_forces(self.h, int(n), int(flags), res.ctypes.data))
+            return res
+        self._check(self.lib.lbmx_step_forces(self.h, int(n), int(flags), out.data_ptr()))
+        return out
 
     def step_sums(self, n, flags=0):
         """n steps that reduce the FP64 sums of every step: an [n, 3] array of

@@ -184,6 +184,16 @@ lbmx_status lbmx_moment_sums_async(lbmx_handle* h, double* sums3);
  * series[4 * k .. 4 * k + 3] = {rho, rho*ux, rho*uy, kinetic energy}. */
 lbmx_status lbmx_step_sums(lbmx_handle* h, int32_t nsteps, uint32_t flags, double* series);
 
+/* nsteps steps (flags as lbmx_step_ex) of a lattice with IBM markers that
+ * also record every step's drag and lift -- minus the marker forces summed
+ * over the markers in FP64, in marker order, as lbmx_ibm_forces returns them
+ * -- into series[2 * k], series[2 * k + 1] for step k.  The IBM kernel writes
+ * them itself when series is device, managed or pinned host memory (the
+ * series is complete once the stream has reached the end); pageable host
+ * memory gets a copy per step.  The reference has no drag or lift; its
+ * marker forces stay on the device (IBMManager.cuh:222-252). */
+lbmx_status lbmx_step_forces(lbmx_handle* h, int32_t nsteps, uint32_t flags, double* series);
+
 /* The kinetic energy 1/2 sum rho |u|^2 (force-corrected u, the velocity
  * lbmx_moments returns) of the last step that reduced the FP64 sums with
  * LBMX_STEP_KINETIC_ENERGY set; 0 when that step's flags did not include it.

@@ -190,6 +190,36 @@ def test_ibm_is_bitwise_reproducible(storage, stencil_quirks):
     assert np.array_equal(Fa, Fb) and np.array_equal(da, db)
 
 
+def test_step_forces_series():
+    """lbmx_step_forces records every step's drag and lift inside the IBM
+    kernel; each entry equals what lbmx_ibm_forces reports after that step,
+    and pageable, pinned and device series are the same bit for bit."""
+    import torch
+
+    mk = C.cylinder_markers(32.3, 24.1, 6.0, 32)
+    c = C.channel(96, 48, markers=mk, u_in=0.05, inlet="parabolic", outlet="zouhe_p")
+    L = C.make_lattice(c)
+    want = []
+    for _ in range(12):
+        L.step(1)
+        want.append(L.marker_forces()[1])
+    want = np.array(want)
+    L2 = C.make_lattice(c)
+    got = L2.step_forces(12)
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-15)
+    L3 = C.make_lattice(c)
+    pinned = torch.zeros(24, dtype=torch.float64).pin_memory()
+    L3.step_forces(12, out=pinned)
+    L3.synchronize()
+    L4 = C.make_lattice(c)
+    dev = torch.zeros(24, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()  # the fill runs on torch's stream, the steps on the lattice's
+    L4.step_forces(12, out=dev)
+    L4.synchronize()
+    assert np.array_equal(pinned.numpy().reshape(12, 2), got)
+    assert np.array_equal(dev.cpu().numpy().reshape(12, 2), got)
+
+
 def test_poiseuille_ibm_reference_scenario():
     # PoiseuilleScenario::add_bodies: cylinder of D=16 at (48, NY/2), 16 markers
     mk = C.cylinder_markers(48.0, 50.0, 8.0, 16)
