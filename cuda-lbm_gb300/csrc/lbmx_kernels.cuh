@@ -45,7 +45,25 @@ constexpr int kThreads = kStepThreads;
 // final conversion.
 using Acc = long long;
 constexpr float kFixScale = 1073741824.0f;  // 2^30
-__device__ __forceinline__ Acc fix(float t) { return __float2ll_rn(t * kFixScale); }
+// round-to-nearest-even of t * 2^30 as a 64-bit integer.  The FP32 -> S64
+// conversion instruction runs on the FP64 pipe, a small fraction of FP32's
+// rate on GB300, so terms below 2048 in magnitude take the FP32 adder
+// instead: adding 1.5 * 2^23 to v (|v| < 2^22) leaves rint(v) in the low
+// mantissa bits.  With x = t * 2^30 (exact), h = rint(x / 2^20) and the
+// remainder r = x - h * 2^20 (exact: |r| <= 2^19, a multiple of x's ulp),
+// rint(x) = h * 2^20 + rint(r) bit for bit, ties to even included, since
+// h * 2^20 is an even integer.  Larger terms and NaN keep the conversion.
+__device__ __forceinline__ Acc fix(float t) {
+    const float x = __fmul_rn(t, kFixScale);
+    if (!(fabsf(t) < 2048.0f)) return __float2ll_rn(x);
+    constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+    const float hb = __fadd_rn(__fmul_rn(x, 9.5367431640625e-07f), kMagic);  // x * 2^-20, rounded to an integer
+    const float hf = __fadd_rn(hb, -kMagic);
+    const float r = __fmaf_rn(-hf, 1048576.0f, x);
+    const int h = __float_as_int(hb) - 0x4B400000;
+    const int lo = __float_as_int(__fadd_rn(r, kMagic)) - 0x4B400000;
+    return ((Acc)h << 20) + (Acc)lo;
+}
 
 // which accumulators a set of sums uses: mass and momentum always, the
 // kinetic energy and the CM_OPT average terms on request
@@ -586,41 +604,93 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
 }
 
 
-// Grid averages <rho>, <rho |u|>, <|Pi|> of the current step before any
-// collision (update_avg_mag, macroscopics.cuh:50-120), for CM_OPT.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) opt_prepass_kernel(const StepArgs a) {
-    Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};
-    const long long n = (long long)a.g.nx * a.g.ny;
-    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads) {
-        const int y = (int)(i / a.g.nx), xx = (int)(i - (long long)y * a.g.nx);
-        {
-            const long long off = (long long)y * a.g.pitch + xx;
-            float f[9];
-            unsigned outmask;
-            gather_node<T>(a, xx, y, f, &outmask);
-            float rho = 0.f, jx = 0.f, jy = 0.f;
+// The CM_OPT average terms of one node from its post-stream, post-boundary
+// populations f: rho, rho |u| (force-corrected u, Brinkman included) and the
+// raw |Pi| (update_avg_mag, macroscopics.cuh:50-120).  One division: u is
+// (j + F/2) times 1 / rho.
+__device__ __forceinline__ void opt_terms(const StepArgs& a, long long off, const float f[9], Acc v[kNumSums]) {
+    float rho = 0.f, jx = 0.f, jy = 0.f;
 #pragma unroll
-            for (int q = 0; q < 9; q++) {
-                rho += f[q];
-                jx += (float)CX(q) * f[q];
-                jy += (float)CY(q) * f[q];
-            }
-            float Fx, Fy;
-            node_force(a, off, &Fx, &Fy);
-            const float inv = 1.0f / rho;
-            float ux = jx * inv + 0.5f * Fx / rho;
-            float uy = jy * inv + 0.5f * Fy / rho;
-            if (a.gamma) brinkman<float>(a.gamma[off], rho, ux, uy, Fx, Fy);
-            const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
-            const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
-            const float pxy = f[5] - f[6] + f[7] - f[8];
-            v[0] += fix(rho);
-            v[4] += fix(rho * sqrtf(ux * ux + uy * uy));
-            v[5] += fix(sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy));
-        }
+    for (int q = 0; q < 9; q++) {
+        rho += f[q];
+        jx += (float)CX(q) * f[q];
+        jy += (float)CY(q) * f[q];
     }
-    block_sums(a, v, (long long)a.g.nx * a.g.ny);
+    float Fx, Fy;
+    node_force(a, off, &Fx, &Fy);
+    const float inv = 1.0f / rho;
+    float ux = fmaf(0.5f, Fx, jx) * inv;
+    float uy = fmaf(0.5f, Fy, jy) * inv;
+    if (a.gamma) brinkman<float>(a.gamma[off], rho, ux, uy, Fx, Fy);
+    const float pxx = f[1] + f[3] + f[5] + f[6] + f[7] + f[8];
+    const float pyy = f[2] + f[4] + f[5] + f[6] + f[7] + f[8];
+    const float pxy = f[5] - f[6] + f[7] - f[8];
+    v[0] += fix(rho);
+    v[4] += fix(rho * sqrtf(ux * ux + uy * uy));
+    v[5] += fix(sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy));
+}
+
+// Grid averages <rho>, <rho |u|>, <|Pi|> of the current step before any
+// collision (update_avg_mag, macroscopics.cuh:50-120), for CM_OPT.  The nodes
+// split as in the step kernel.  Units the tiles take (special bit clear; in a
+// neighbour-access step also off the perimeter) load their 18 populations
+// directly, one unit of two x-neighbours per thread over row segments of
+// 2 * kThreads nodes; the pairs that do not shift in x are single aligned
+// loads.  The parity's general-path units are spread over every thread of
+// the grid, one node each, through the general path.  The terms are summed
+// in exact fixed point, so the averages do not depend on the order.
+template <typename T>
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) opt_prepass_kernel(const StepArgs a) {
+    Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};
+    const Geometry& g = a.g;
+    const T* F = static_cast<const T*>(a.f);
+    const int seg_w = 2 * kThreads;
+    const int segs = (g.nx + seg_w - 1) / seg_w;
+    const int items = segs * g.ny;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+        const int y = it / segs;
+        const int x0 = (it - y * segs) * seg_w + 2 * (int)threadIdx.x;
+        if (x0 + 1 >= g.nx) continue;  // a lone last node is a general-path unit
+        if (a.parity && !(y > 0 && y < g.ny - 1 && x0 > 0 && x0 + 1 < g.nx - 1)) continue;
+        const long long n0 = (long long)y * g.pitch + x0;
+        if (a.special_bits) {
+            const long long unit = n0 >> 1;
+            if ((a.special_bits[unit >> 5] >> (unit & 31)) & 1u) continue;
+        }
+        float f0[9], f1[9];
+        const float2 r = Store<T>::ld2(F + a.rest_plane * g.plane + n0, WQ(0));
+        f0[0] = r.x;
+        f1[0] = r.y;
+#pragma unroll
+        for (int q = 1; q < 9; q++) {
+            if (!a.parity) {
+                const float2 p = Store<T>::ld2(F + q * g.plane + n0, WQ(q));
+                f0[q] = p.x;
+                f1[q] = p.y;
+            } else if (CX(q) == 0) {
+                const float2 p = Store<T>::ld2(F + OPP(q) * g.plane + n0 - CY(q) * g.pitch, WQ(q));
+                f0[q] = p.x;
+                f1[q] = p.y;
+            } else {
+                const T* src = F + OPP(q) * g.plane + n0 - CY(q) * g.pitch - CX(q);
+                f0[q] = Store<T>::ld(src, WQ(q));
+                f1[q] = Store<T>::ld(src + 1, WQ(q));
+            }
+        }
+        opt_terms(a, n0, f0, v);
+        opt_terms(a, n0 + 1, f1, v);
+    }
+    const int nthreads = gridDim.x * kThreads;
+    for (int k = blockIdx.x * kThreads + threadIdx.x; k < 2 * a.nspecial; k += nthreads) {
+        const int off = a.special_units[k >> 1] + (k & 1);
+        const int y = off / g.pitch, x = off - y * g.pitch;
+        if (x >= g.nx) continue;
+        float f[9];
+        unsigned outmask;
+        gather_node<T>(a, x, y, f, &outmask);
+        opt_terms(a, off, f, v);
+    }
+    block_sums(a, v, (long long)g.nx * g.ny);
 }
 
 __device__ __forceinline__ void edge_coords(int e, int nx, int ny, int* x, int* y) {
