@@ -819,25 +819,29 @@ __global__ void get_populations_kernel(const StepArgs a, float* out, int last_pa
 // The IBM of one step in one CTA: density and uncorrected velocity of the
 // patch nodes (the reference interpolates from d_rho and the copy of d_u
 // taken before the force correction, IBMManager.cuh:227-228), gathered
-// straight into shared memory, then the multi-direct rounds (ibm_iterate,
-// lbmx_ibm.cuh).  The stencils and spread lists do not depend on the flow, so
-// they are staged before the wait for the previous step.  Launched with
-// programmatic stream serialization like the step kernel: it waits for the
-// previous step before reading the populations and lets the next step kernel
-// launch and wait behind it.
+// straight into shared memory, then the multi-direct rounds
+// (ibm_fast_iterate, lbmx_ibm.cuh).  The stencils, spread lists, patch node
+// offsets and flags do not depend on the flow, so they are staged before the
+// wait for the previous step.  Launched with programmatic stream
+// serialization like the step kernel: it waits for the previous step before
+// reading the populations and lets the next step kernel launch and wait
+// behind it.
 template <typename T>
 __global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a, const IbmArgs ib) {
-    extern __shared__ float sm[];
-    const IbmSmem<float> s = ibm_layout(ib, sm);
-    ibm_stage(ib, s);
+    extern __shared__ float4 sm4[];
+    const IbmFast s = ibm_fast_layout(ib, sm4);
+    ibm_fast_stage(ib, s, a.flags);
+    __syncthreads();
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" :::);
     for (int i = threadIdx.x; i < ib.npatch; i += blockDim.x) {
-        const int off = ib.patch_nodes[i];
+        const int off = s.pn[i];
+        const uint8_t fl = s.pf[i];
         const int y = off / a.g.pitch, x = off - y * a.g.pitch;
         float f[9];
         unsigned m;
-        gather_node<T>(a, x, y, f, &m);
+        load_post_stream<T>(a, x, y, fl, f, &m);  // gather_node with the staged flag
+        if (fl) apply_bc(a, f, x, y, fl);
         float rho = 0.f, jx = 0.f, jy = 0.f;
 #pragma unroll
         for (int q = 0; q < 9; q++) {
@@ -846,17 +850,18 @@ __global__ void __launch_bounds__(kIbmThreads) ibm_step_kernel(const StepArgs a,
             jy += (float)CY(q) * f[q];
         }
         const float inv = 1.0f / rho;
-        ibm_set_patch(s, i, rho, jx * inv, jy * inv);
+        s.ps[i] = make_float4(jx * inv, jy * inv, rho, 1.0f / (2.0f * rho));
     }
     __syncthreads();
-    ibm_iterate(ib, s);
+    ibm_fast_iterate(ib, s);
     // drag and lift of the step: minus the summed marker forces, in FP64,
     // each lane taking every 32nd marker, then a fixed shuffle tree
     if (ib.force_series && threadIdx.x < 32) {
         double dx = 0.0, dy = 0.0;
         for (int k = threadIdx.x; k < ib.nm; k += 32) {
-            dx += (double)s.mtx[k];
-            dy += (double)s.mty[k];
+            const float2 m = s.mt[k];
+            dx += (double)m.x;
+            dy += (double)m.y;
         }
         for (int o = 16; o > 0; o >>= 1) {
             dx += __shfl_xor_sync(0xffffffffu, dx, o);
@@ -953,7 +958,7 @@ cudaError_t launch_get_populations(const StepArgs& a, float* out, cudaStream_t s
 template <typename T>
 cudaError_t launch_ibm_step(const StepArgs& a, const IbmArgs& ib, cudaStream_t s) {
     if (ib.npatch <= 0) return cudaSuccess;
-    const size_t smem = ibm_smem_bytes_of<float>(ib.npatch, ib.nm, ib.stencil);
+    const size_t smem = ibm_fast_smem_bytes(ib.npatch, ib.nm, ib.stencil);
     // the attribute grows with the patch: raise it when a larger one comes
     static int configured[64] = {0};
     int dev = 0;
