@@ -108,6 +108,7 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.error_word = h->error_word;
     a.tile_chunk = h->tile_chunk;
     a.sr = (h->p.storage != LBMX_STORAGE_F32 && !(h->p.options & LBMX_OPTION_ROUND_NEAREST)) ? 1 : 0;
+    a.sr_unit_origin = (uint32_t)((unsigned long long)(h->row_origin * h->g.pitch) >> 1);
     return a;
 }
 
@@ -144,12 +145,26 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     };
     std::vector<int> units, units0;
     std::vector<uint32_t> bits(((size_t)g.ny * units_per_row + 31) / 32, 0u), bits0(bits.size(), 0u);
+    // ghost rows (a y-slab's copies of its neighbours' boundary rows) are in
+    // no unit list; parity 0 marks them so the tiles skip them too, parity 1
+    // tiles skip them as perimeter rows
+    const auto ghost = [&](int y) {
+        return ((h->ghost_mask & 1u) && y == 0) || ((h->ghost_mask & 2u) && y == g.ny - 1);
+    };
     for (int y = 0; y < g.ny; y++)
         for (int x0 = 0; x0 < g.nx; x0 += 2) {
             const bool perim = y == 0 || y == g.ny - 1 || x0 == 0 || x0 + 1 >= g.nx - 1;
             const size_t u = (size_t)y * units_per_row + x0 / 2;
-            if (perim || interior_special[u]) units.push_back(y * g.pitch + x0);
-            if (!perim && interior_special[u]) {
+            if (ghost(y)) {
+                bits0[u >> 5] |= 1u << (u & 31);
+                continue;
+            }
+            // a y-slab of a y-periodic lattice: the lattice's first and last
+            // rows take the general path of a neighbour-access step, as there
+            const long long wy = h->whole_ny > 0 ? ((h->row_origin + y) % h->whole_ny + h->whole_ny) % h->whole_ny : -1;
+            const bool wrap_row = h->whole_ny > 0 && (wy == 0 || wy == h->whole_ny - 1);
+            if (perim || interior_special[u] || wrap_row) units.push_back(y * g.pitch + x0);
+            if (!perim && (interior_special[u] || wrap_row)) {
                 bits[u >> 5] |= 1u << (u & 31);
                 any_interior = true;
             }
@@ -171,8 +186,9 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
         LBMX_CUDA(h, cudaMemcpy(h->special_bits, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
     LBMX_CUDA(h, cudaMalloc((void**)&h->special_units0, std::max<size_t>(1, units0.size()) * sizeof(int)));
-    if (!units0.empty()) {
+    if (!units0.empty())
         LBMX_CUDA(h, cudaMemcpy(h->special_units0, units0.data(), units0.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!units0.empty() || h->ghost_mask) {
         LBMX_CUDA(h, cudaMalloc((void**)&h->special_bits0, bits0.size() * sizeof(uint32_t)));
         LBMX_CUDA(h, cudaMemcpy(h->special_bits0, bits0.data(), bits0.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
@@ -276,7 +292,7 @@ void lbmx_destroy(lbmx_handle* h) {
     free_ibm(h);
     cudaFree(h->f_alloc); cudaFree(h->flags); cudaFree(h->edge); cudaFree(h->aux);
     cudaFree(h->force); cudaFree(h->gamma); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
-    cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums);
+    cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums); cudaFree(h->raw_sums);
     cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
     cudaFree(h->special_units0); cudaFree(h->special_bits0);
     cudaFree(h->tile_counter);
@@ -554,8 +570,10 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, b
                   }));
     }
     const bool opt = h->p.op == LBMX_CM_OPT;
-    const bool lagged = opt && (h->p.options & LBMX_OPTION_LAGGED_AVERAGES) && h->have_avg;
-    if (opt && !lagged) {
+    const bool ext = opt && h->ext_avg;
+    h->ext_avg = false;
+    const bool lagged = opt && !ext && (h->p.options & LBMX_OPTION_LAGGED_AVERAGES) && h->have_avg;
+    if (opt && !lagged && !ext) {
         StepArgs b = a;
         b.partials = acc;
         b.counter = h->counter;
@@ -783,6 +801,105 @@ lbmx_status lbmx_get_populations(lbmx_handle* h, float* out) {
     return LBMX_OK;
 }
 
+// ---------------------------------------------------------------- y-slabs
+lbmx_status lbmx_set_slab(lbmx_handle* h, uint32_t ghost_mask, int64_t row_origin, int32_t whole_ny) {
+    if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_slab: NULL handle");
+    if (ghost_mask > 3u)
+        return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_slab: ghost mask %u (bits 0 and 1 only)", ghost_mask);
+    if (ghost_mask && h->g.periodic_y)
+        return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_slab: a lattice with ghost rows is not periodic in y");
+    if (h->g.ny < 3) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_slab: ny < 3");
+    if (ghost_mask && h->nm > 0) return fail(h, LBMX_ERR_UNSUPPORTED, "lbmx_set_slab: IBM markers on a y-slab");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (whole_ny < 0 || (whole_ny > 0 && whole_ny < h->g.ny - 2))
+        return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_slab: whole_ny %d", whole_ny);
+    h->ghost_mask = ghost_mask;
+    h->row_origin = row_origin;
+    h->whole_ny = whole_ny;
+    return rebuild_special(h);
+}
+
+// Raw slot copies of one row: for each population q in plane_mask
+// (ascending), nx stored elements of plane q, row `row`.
+static lbmx_status halo_copy(lbmx_handle* h, int32_t row, uint32_t plane_mask, void* buf, bool get, const char* who) {
+    if (!h || !buf) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "%s: NULL argument", who);
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "%s: not initialized", who);
+    if (row < 0 || row >= h->g.ny || plane_mask == 0 || plane_mask > 0x1FFu)
+        return fail(h, LBMX_ERR_INVALID_ARGUMENT, "%s: row %d or plane mask 0x%x out of range", who, row, plane_mask);
+    cudaSetDevice(h->p.device);
+    const size_t es = elem_size(h->p.storage), bytes = (size_t)h->g.nx * es;
+    char* f = static_cast<char*>(h->f);
+    char* b = static_cast<char*>(buf);
+    static const int cx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    for (int q = 0; q < 9; q++) {
+        if (!((plane_mask >> q) & 1u)) continue;
+        char* slot = f + ((size_t)q * h->g.plane + (size_t)row * h->g.pitch) * es;
+        // a put writes only the slots a node of the neighbouring row writes in
+        // a neighbour-access step: on a lattice not periodic in x, slot q of
+        // the column whose upstream column x - c_q is outside belongs to the
+        // node itself (a half-way wall reflects into it)
+        size_t skip_lo = 0, skip_hi = 0;
+        if (!get && !h->g.periodic_x) {
+            if (cx[q] > 0) skip_lo = 1;
+            if (cx[q] < 0) skip_hi = 1;
+        }
+        const size_t n = bytes - (skip_lo + skip_hi) * es;
+        if (get)
+            LBMX_CUDA(h, cudaMemcpyAsync(b, slot, bytes, cudaMemcpyDefault, h->stream));
+        else
+            LBMX_CUDA(h, cudaMemcpyAsync(slot + skip_lo * es, b + skip_lo * es, n, cudaMemcpyDefault, h->stream));
+        b += bytes;
+    }
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_halo_get(lbmx_handle* h, int32_t row, uint32_t plane_mask, void* buf) {
+    return halo_copy(h, row, plane_mask, buf, true, "lbmx_halo_get");
+}
+
+lbmx_status lbmx_halo_put(lbmx_handle* h, int32_t row, uint32_t plane_mask, const void* buf) {
+    return halo_copy(h, row, plane_mask, const_cast<void*>(buf), false, "lbmx_halo_put");
+}
+
+lbmx_status lbmx_opt_partials(lbmx_handle* h, int64_t* sums3) {
+    if (!h || !sums3) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_opt_partials: NULL argument");
+    if (!h->initialized) return fail(h, LBMX_ERR_NOT_INITIALIZED, "lbmx_opt_partials: not initialized");
+    if (h->p.op != LBMX_CM_OPT) return fail(h, LBMX_ERR_UNSUPPORTED, "lbmx_opt_partials: the operator is not CM_OPT");
+    cudaSetDevice(h->p.device);
+    if (!h->raw_sums) LBMX_CUDA(h, cudaMalloc((void**)&h->raw_sums, kNumSums * sizeof(long long)));
+    const long long s = h->t + 1;
+    StepArgs a = base_args(h);
+    set_step(h, a, s);
+    if (h->has_aux_bc)
+        LBMX_CUDA(h, dispatch(h->p.storage, [&](auto tag) { return launch_edge_prepass<decltype(tag)>(a, h->aux, h->stream); }));
+    StepArgs b = a;
+    b.partials = h->partials + (size_t)(s & 1) * kAccPerSet;
+    b.counter = h->counter;
+    b.sums = nullptr;
+    b.avg_out = h->avg;
+    b.raw_sums = h->raw_sums;
+    LBMX_CUDA(h, dispatch(h->p.storage, [&](auto tag) { return launch_opt_prepass<decltype(tag)>(b, h->stream); }));
+    long long r[kNumSums];
+    LBMX_CUDA(h, cudaMemcpyAsync(r, h->raw_sums, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    sums3[0] = r[0];
+    sums3[1] = r[4];
+    sums3[2] = r[5];
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_set_averages(lbmx_handle* h, const float* avg3) {
+    if (!h || !avg3) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_set_averages: NULL argument");
+    if (h->p.op != LBMX_CM_OPT) return fail(h, LBMX_ERR_UNSUPPORTED, "lbmx_set_averages: the operator is not CM_OPT");
+    cudaSetDevice(h->p.device);
+    LBMX_CUDA(h, cudaMemcpyAsync(h->avg, avg3, 3 * sizeof(float), cudaMemcpyDefault, h->stream));
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->ext_avg = true;
+    h->have_avg = true;
+    return LBMX_OK;
+}
+
 lbmx_status lbmx_averages(lbmx_handle* h, float* avg3) {
     if (!h || !avg3) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_averages: NULL argument");
     cudaSetDevice(h->p.device);
@@ -853,6 +970,7 @@ extern "C" {
 lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n) {
     if (!h) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: NULL handle");
     if (n < 0 || (n > 0 && !xy)) return fail(h, LBMX_ERR_INVALID_ARGUMENT, "lbmx_ibm_set_markers: bad marker array");
+    if (n > 0 && h->ghost_mask) return fail(h, LBMX_ERR_UNSUPPORTED, "lbmx_ibm_set_markers: IBM markers on a y-slab");
     cudaSetDevice(h->p.device);
     LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
     free_ibm(h);

@@ -312,7 +312,7 @@ __device__ __forceinline__ void store_post_collision(const StepArgs& a, int x, i
     const long long row = (long long)y * g.pitch;
     const bool hw = is_halfway(fl);
     const bool sr = kOffset<T> && a.sr;
-    const uint32_t h = sr ? sr_hash((uint32_t)(row + x) >> 1, seed) : 0u;
+    const uint32_t h = sr ? sr_hash(((uint32_t)(row + x) >> 1) + a.sr_unit_origin, seed) : 0u;
     const int lane = (int)((row + x) & 1);
     // the value f of population q goes to p, rounded as configured (the
     // node's half of its unit's random bits)

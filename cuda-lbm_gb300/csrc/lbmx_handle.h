@@ -36,6 +36,11 @@ struct lbmx_handle {
     long long t = 0;
     bool initialized = false;
     bool have_avg = false;
+    bool ext_avg = false;          // the next step uses averages set by lbmx_set_averages
+    uint32_t ghost_mask = 0;       // bit 0: row 0, bit 1: row ny-1 is a ghost row (never stepped)
+    long long row_origin = 0;      // row of the whole lattice that handle row 0 stands for (y-slabs)
+    int whole_ny = 0;              // rows of a y-periodic whole lattice (y-slabs), else 0
+    long long* raw_sums = nullptr; // [kNumSums] integer sums of lbmx_opt_partials
     // immersed boundary
     int nm = 0, npatch = 0, stencil = 0;
     int* patch_nodes = nullptr;

@@ -52,6 +52,7 @@ struct StepArgs {
     int rest_plane;          // plane that holds f0 this step (0 or 9)
     int sr;                  // 16-bit stores round stochastically (else to nearest)
     uint32_t sr_seed;        // sr_seed_of(step index) for the rounding hash
+    uint32_t sr_unit_origin; // added to a node's unit offset in the rounding hash (a y-slab's rows in the whole lattice)
     long long st_off[9];     // byte offset, from a node's plane-0 element, of the slot its q-th
                              // post-collision population goes to this step (interior nodes)
     float omega;
@@ -83,6 +84,7 @@ struct StepArgs {
     double* pub_acc;
     double* pub_sums;
     double* pub_series;
+    long long* raw_sums;     // or null: the last CTA also writes the integer fixed-point sums [kNumSums]
 };
 
 // Seed of the stochastic-rounding hash for step index s (a Weyl sequence:

@@ -90,10 +90,12 @@ __device__ __forceinline__ void warp_sums(double* partials, const Acc v[kNumSums
 
 // The sums in `mask` of an accumulator set (integer sums over the slots: the
 // same bits in any order), zeroing them for their next use; the others are 0.
-__device__ __forceinline__ void collect_sums(double* partials, unsigned mask, double s[kNumSums]) {
+__device__ __forceinline__ void collect_sums(double* partials, unsigned mask, double s[kNumSums],
+                                             long long* raw = nullptr) {
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials);
     for (int k = 0; k < kNumSums; k++) {
         s[k] = 0.0;
+        if (raw) raw[k] = 0;
         if (!((mask >> k) & 1u)) continue;
         unsigned long long t = 0;
         for (int j = 0; j < kSumSlots; j++) {
@@ -101,6 +103,7 @@ __device__ __forceinline__ void collect_sums(double* partials, unsigned mask, do
             acc[j * kNumSums + k] = 0ull;
         }
         s[k] = (double)(long long)t * (1.0 / (double)kFixScale);
+        if (raw) raw[k] = (long long)t;
     }
 }
 
@@ -139,7 +142,7 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[kNumSu
     if (!is_last || tid != 0) return;
     __threadfence();
     double s[kNumSums];
-    collect_sums(a.partials, mask, s);
+    collect_sums(a.partials, mask, s, a.raw_sums);
     write_sums(s, a.sums, a.series, a.ke != 0);
     if (a.avg_out) {
         a.avg_out[0] = (float)(s[0] / (double)n_nodes);
@@ -430,7 +433,7 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     char* base = reinterpret_cast<char*>(F + off);
     if (OFS && a.sr) {
         // stochastic rounding, random bits from each node's hash
-        const uint32_t h = sr_hash((uint32_t)off >> 1, seed);
+        const uint32_t h = sr_hash(((uint32_t)off >> 1) + a.sr_unit_origin, seed);
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             T* p = reinterpret_cast<T*>(base + a.st_off[q]);

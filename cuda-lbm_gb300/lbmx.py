@@ -42,7 +42,8 @@ EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy"
             "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward", "lbmx_adjoint_moments",
             "lbmx_adjoint_last_error", "lbmx_tangent_create", "lbmx_tangent_destroy", "lbmx_tangent_set_state",
             "lbmx_tangent_set_markers", "lbmx_tangent_run", "lbmx_tangent_moments", "lbmx_tangent_time",
-            "lbmx_tangent_last_error"]
+            "lbmx_tangent_last_error", "lbmx_set_slab", "lbmx_halo_get", "lbmx_halo_put",
+            "lbmx_opt_partials", "lbmx_set_averages"]
 # lbmx_tangent_create parameters
 TANGENT_U_BC, TANGENT_OMEGA, TANGENT_BODY_FX, TANGENT_WALL_UX = 0, 1, 2, 3
 
@@ -98,6 +99,13 @@ def load_library(path=LIB_PATH):
     lib.lbmx_moment_sums_async.restype = ctypes.c_int32
     lib.lbmx_step_sums.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
     lib.lbmx_step_sums.restype = ctypes.c_int32
+    lib.lbmx_set_slab.argtypes = [vp, ctypes.c_uint32, ctypes.c_int64, ctypes.c_int32]
+    lib.lbmx_halo_get.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
+    lib.lbmx_halo_put.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
+    lib.lbmx_opt_partials.argtypes = [vp, P(ctypes.c_int64)]
+    lib.lbmx_set_averages.argtypes = [vp, fp]
+    for name in ("lbmx_set_slab", "lbmx_halo_get", "lbmx_halo_put", "lbmx_opt_partials", "lbmx_set_averages"):
+        getattr(lib, name).restype = ctypes.c_int32
     lib.lbmx_step_forces.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32, vp]
     lib.lbmx_step_forces.restype = ctypes.c_int32
     lib.lbmx_kinetic_energy.argtypes = [vp, vp]
@@ -212,6 +220,8 @@ class Lattice:
         self.h = h
         self.nx, self.ny, self.n = nx, ny, nx * ny
         self.nm = 0
+        self.op = op
+        self.elem_size = 4 if storage == F32 else 2
 
     def close(self):
         if getattr(self, "h", None):
@@ -245,6 +255,30 @@ class Lattice:
 
     def step(self, n=1, flags=STEP_STORE_MOMENTS):
         self._check(self.lib.lbmx_step_ex(self.h, int(n), int(flags)))
+
+    # --- y-slabs (lbmx_set_slab, lbmx_halo_*, lbmx_opt_partials, lbmx_set_averages)
+    def set_slab(self, ghost_mask, row_origin, whole_ny=0):
+        self._check(self.lib.lbmx_set_slab(self.h, int(ghost_mask), int(row_origin), int(whole_ny)))
+
+    def halo_get(self, row, plane_mask, buf):
+        """Copy the stored slots of `row`, planes in plane_mask, into buf (a
+        contiguous numpy array or torch tensor of the storage's element size)."""
+        ptr = buf.data_ptr() if hasattr(buf, "data_ptr") else buf.ctypes.data
+        self._check(self.lib.lbmx_halo_get(self.h, int(row), int(plane_mask), ptr))
+        return buf
+
+    def halo_put(self, row, plane_mask, buf):
+        ptr = buf.data_ptr() if hasattr(buf, "data_ptr") else buf.ctypes.data
+        self._check(self.lib.lbmx_halo_put(self.h, int(row), int(plane_mask), ptr))
+
+    def opt_partials(self):
+        out = (ctypes.c_int64 * 3)()
+        self._check(self.lib.lbmx_opt_partials(self.h, out))
+        return np.array(list(out), np.int64)
+
+    def set_averages(self, avg3):
+        a = (ctypes.c_float * 3)(*[float(v) for v in avg3])
+        self._check(self.lib.lbmx_set_averages(self.h, a))
 
     def step_forces(self, n, flags=0, out=None):
         """n steps recording each step's drag and lift (lbmx_step_forces):

@@ -214,6 +214,56 @@ lbmx_status lbmx_get_populations(lbmx_handle* h, float* out);
  * reference's d_moment_avg, src/core/lbm.cu:19); computed for CM_OPT only. */
 lbmx_status lbmx_averages(lbmx_handle* h, float* avg3);
 
+/* --- y-slab decomposition.  No counterpart in the reference, which runs one
+ * lattice on one device (src/main.cu:39-41).  A lattice of NY rows is split
+ * into slabs of whole rows, one handle each, whose lattice adds a ghost row
+ * on each side that has a neighbouring slab: a copy of that neighbour's
+ * boundary row.  Ghost rows are never stepped.  In a neighbour-access step
+ * (odd step index) a boundary row reads three populations from its ghost row
+ * and writes three into it, so each slab, around that step:
+ *   before: fills its lower ghost row's planes 4, 7, 8 and its upper ghost
+ *           row's planes 2, 5, 6 from the neighbours' boundary rows;
+ *   after:  returns its lower ghost row's planes 4, 7, 8 and its upper ghost
+ *           row's planes 2, 5, 6 into the neighbours' boundary rows.
+ * An own-node step (even index) exchanges nothing.  With CM_OPT the slabs'
+ * integer average sums (lbmx_opt_partials) are added over all slabs and the
+ * averages set on each (lbmx_set_averages) before every step, so a split
+ * lattice steps bit for bit as the whole one, 16-bit storage included.
+ * cuda-lbm_gb300/lbmx_slabs.py drives this protocol. */
+
+/* Makes the handle a y-slab: row 0 (ghost_mask bit 0) and row ny-1 (bit 1)
+ * are ghost rows, and handle row 0 stands for row row_origin of the whole
+ * lattice (the stochastic-rounding hash uses whole-lattice node offsets, so
+ * 16-bit storage rounds as in the whole lattice).  whole_ny: the whole
+ * lattice's row count when it is periodic in y, else 0 -- its first and last
+ * rows then take the general path in neighbour-access steps, as they do in
+ * the whole lattice.  The slab's own lattice must not be periodic in y (the
+ * ghost rows carry the wrap) and carries no IBM markers. */
+lbmx_status lbmx_set_slab(lbmx_handle* h, uint32_t ghost_mask, int64_t row_origin, int32_t whole_ny);
+
+/* Copy the stored slots of row `row`, population planes in plane_mask
+ * (ascending q), nx stored elements each (4 bytes for FP32 storage, 2 for
+ * the 16-bit offset forms), out to buf / in from buf, on the handle's stream:
+ * device, managed or pinned buf is stream-ordered; pageable host memory is
+ * copied before the call returns.  A put writes only the slots that a node of
+ * the neighbouring row writes in a neighbour-access step: on a lattice not
+ * periodic in x it leaves slot q of the column whose upstream column x - c_q
+ * lies outside the lattice (a half-way wall node reflects into that slot
+ * itself). */
+lbmx_status lbmx_halo_get(lbmx_handle* h, int32_t row, uint32_t plane_mask, void* buf);
+lbmx_status lbmx_halo_put(lbmx_handle* h, int32_t row, uint32_t plane_mask, const void* buf);
+
+/* CM_OPT: the integer fixed-point sums (units of 2^-30) of rho, rho|u| and
+ * |Pi| over the stepped nodes for the next step, the terms of its grid
+ * averages (update_avg_mag, macroscopics.cuh:50-120).  Adding the sums of
+ * all slabs gives exactly the whole lattice's. */
+lbmx_status lbmx_opt_partials(lbmx_handle* h, int64_t* sums3);
+
+/* CM_OPT: the next step uses these averages {<rho>, <rho|u|>, <|Pi|>}
+ * instead of computing its own.  The whole lattice's are
+ * (float)((double)sum * 2^-30 / (double)nodes) of the summed partials. */
+lbmx_status lbmx_set_averages(lbmx_handle* h, const float* avg3);
+
 /* Replaces IBMManager<2>::init_and_dispatch (src/IBM/IBMManager.cuh:54-109):
  * n static markers, xy[2n] interleaved (the reference's IBMBody.points). */
 lbmx_status lbmx_ibm_set_markers(lbmx_handle* h, const float* xy, int32_t n);
