@@ -61,6 +61,7 @@ struct AdjArgs {
     const uint8_t* flags;   // [n] or null
     const float* gamma;     // [n] or null
     const float* weights;   // [3][n] objective weights or null
+    int drag;               // the objective's node terms are multiplied by the node's gamma
 };
 
 __device__ __forceinline__ bool adj_halfway(uint8_t fl) { return fl == LBMX_MOVING_WALL_BB || fl == LBMX_HALFWAY_BB; }
@@ -245,9 +246,11 @@ __global__ void adj_forward_kernel(const AdjArgs a, const float* pc_prev, float*
     adj_node<float, OP>(a, f, a.gamma ? a.gamma[node] : 0.0f, a.fx, a.fy, a.omega, a.S, av, mom);
 #pragma unroll
     for (int q = 0; q < 9; q++) pc_next[q * n + node] = f[q];
-    if (objective && a.weights)
-        jnode[node] += (double)a.weights[node] * mom[0] + (double)a.weights[n + node] * (mom[0] * mom[1]) +
-                       (double)a.weights[2 * n + node] * (mom[0] * mom[2]);
+    if (objective && a.weights) {
+        const double term = (double)a.weights[node] * mom[0] + (double)a.weights[n + node] * (mom[0] * mom[1]) +
+                            (double)a.weights[2 * n + node] * (mom[0] * mom[2]);
+        jnode[node] += a.drag ? (double)(a.gamma ? a.gamma[node] : 0.0f) * term : term;
+    }
     if (rho_out) {
         rho_out[node] = mom[0];
         u_out[node] = mom[1];
@@ -328,7 +331,15 @@ __global__ void __launch_bounds__(kAdjBlock, kAdjReverseBlocksPerSm) adj_reverse
 #pragma unroll
             for (int k = 0; k < kTan; k++) {
                 if (p0 + k >= D) break;
-                float t = w[0] * mom[0].d[k] + w[1] * jx.d[k] + w[2] * jy.d[k];
+                float t;
+                if (a.drag) {
+                    // J's node term gamma (w . moments): its gamma column
+                    // gains the explicit term w . moments
+                    const R ob = g * (w[0] * mom[0] + w[1] * jx + w[2] * jy);
+                    t = ob.d[k];
+                } else {
+                    t = w[0] * mom[0].d[k] + w[1] * jx.d[k] + w[2] * jy.d[k];
+                }
                 float tsum = 0.0f;
 #pragma unroll
                 for (int q = 0; q < 9; q++) {
@@ -700,8 +711,19 @@ lbmx_status lbmx_adjoint_set_objective(lbmx_adjoint* a, const float* weights, in
     ADJ_CUDA(a, cudaMemcpyAsync(a->weights, weights, (size_t)3 * a->n * sizeof(float), cudaMemcpyDefault, a->stream));
     ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
     a->args.weights = a->weights;
+    a->args.drag = 0;
     a->first = first_step;
     a->have_forward = false;
+    return LBMX_OK;
+}
+
+lbmx_status lbmx_adjoint_set_objective_ex(lbmx_adjoint* a, const float* weights, int32_t first_step, int32_t kind) {
+    if (!a) return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_objective_ex: NULL handle");
+    if (kind != LBMX_OBJECTIVE_MOMENTS && kind != LBMX_OBJECTIVE_BRINKMAN_DRAG)
+        return afail(a, LBMX_ERR_INVALID_ARGUMENT, "lbmx_adjoint_set_objective_ex: kind %d", kind);
+    const lbmx_status st = lbmx_adjoint_set_objective(a, weights, first_step);
+    if (st != LBMX_OK) return st;
+    a->args.drag = kind == LBMX_OBJECTIVE_BRINKMAN_DRAG ? 1 : 0;
     return LBMX_OK;
 }
 

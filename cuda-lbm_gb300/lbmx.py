@@ -39,11 +39,13 @@ EXPORTED = ["lbmx_version", "lbmx_params_default", "lbmx_create", "lbmx_destroy"
             "lbmx_batch_set_config", "lbmx_batch_get_config", "lbmx_batch_autotune", "lbmx_batch_step",
             "lbmx_batch_synchronize", "lbmx_batch_last_error", "lbmx_adjoint_create", "lbmx_adjoint_destroy",
             "lbmx_adjoint_set_state", "lbmx_adjoint_set_gamma", "lbmx_adjoint_set_scalars",
-            "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward", "lbmx_adjoint_moments",
+            "lbmx_adjoint_set_objective", "lbmx_adjoint_set_objective_ex", "lbmx_adjoint_forward", "lbmx_adjoint_backward", "lbmx_adjoint_moments",
             "lbmx_adjoint_last_error", "lbmx_tangent_create", "lbmx_tangent_destroy", "lbmx_tangent_set_state",
             "lbmx_tangent_set_markers", "lbmx_tangent_run", "lbmx_tangent_moments", "lbmx_tangent_time",
             "lbmx_tangent_last_error", "lbmx_set_slab", "lbmx_halo_get", "lbmx_halo_put",
             "lbmx_opt_partials", "lbmx_set_averages"]
+# lbmx_adjoint_set_objective_ex kinds
+OBJECTIVE_MOMENTS, OBJECTIVE_BRINKMAN_DRAG = 0, 1
 # lbmx_tangent_create parameters
 TANGENT_U_BC, TANGENT_OMEGA, TANGENT_BODY_FX, TANGENT_WALL_UX = 0, 1, 2, 3
 
@@ -140,6 +142,7 @@ def load_library(path=LIB_PATH):
     lib.lbmx_adjoint_set_gamma.argtypes = [vp, vp]
     lib.lbmx_adjoint_set_scalars.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float]
     lib.lbmx_adjoint_set_objective.argtypes = [vp, vp, ctypes.c_int32]
+    lib.lbmx_adjoint_set_objective_ex.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32]
     lib.lbmx_adjoint_forward.argtypes = [vp, ctypes.c_int32, dp]
     lib.lbmx_adjoint_backward.argtypes = [vp, vp, dp]
     lib.lbmx_adjoint_moments.argtypes = [vp, vp, vp]
@@ -156,7 +159,7 @@ def load_library(path=LIB_PATH):
     lib.lbmx_tangent_last_error.restype = ctypes.c_char_p
     lib.lbmx_tangent_last_error.argtypes = [vp]
     for name in ("lbmx_adjoint_create", "lbmx_adjoint_set_state", "lbmx_adjoint_set_gamma", "lbmx_adjoint_set_scalars",
-                 "lbmx_adjoint_set_objective", "lbmx_adjoint_forward", "lbmx_adjoint_backward",
+                 "lbmx_adjoint_set_objective", "lbmx_adjoint_set_objective_ex", "lbmx_adjoint_forward", "lbmx_adjoint_backward",
                  "lbmx_adjoint_moments"):
         getattr(lib, name).restype = ctypes.c_int32
     lib.lbmx_moment_sums_noalloc.restype = ctypes.c_int32
@@ -458,9 +461,12 @@ class Adjoint:
     def set_scalars(self, omega, fx, fy):
         self._check(self.lib.lbmx_adjoint_set_scalars(self.a, float(omega), float(fx), float(fy)))
 
-    def set_objective(self, weights, first_step):
+    def set_objective(self, weights, first_step, kind=OBJECTIVE_MOMENTS):
         pw, k = _ptr(weights, np.float32)
-        self._check(self.lib.lbmx_adjoint_set_objective(self.a, pw, int(first_step)))
+        if kind == OBJECTIVE_MOMENTS:
+            self._check(self.lib.lbmx_adjoint_set_objective(self.a, pw, int(first_step)))
+        else:
+            self._check(self.lib.lbmx_adjoint_set_objective_ex(self.a, pw, int(first_step), int(kind)))
 
     def forward(self, nsteps):
         J = ctypes.c_double()

@@ -349,6 +349,15 @@ lbmx_status lbmx_adjoint_set_gamma(lbmx_adjoint* a, const float* gamma);
 lbmx_status lbmx_adjoint_set_scalars(lbmx_adjoint* a, float omega, float body_fx, float body_fy);
 /* weights[3n]: w_rho, w_x, w_y planes */
 lbmx_status lbmx_adjoint_set_objective(lbmx_adjoint* a, const float* weights, int32_t first_step);
+/* Objective kinds of lbmx_adjoint_set_objective_ex. */
+enum { LBMX_OBJECTIVE_MOMENTS = 0, LBMX_OBJECTIVE_BRINKMAN_DRAG = 1 };
+/* As lbmx_adjoint_set_objective; with LBMX_OBJECTIVE_BRINKMAN_DRAG each
+ * node's term is multiplied by its Brinkman fraction:
+ * J = sum over t >= first, x of gamma (w_rho rho + w_x rho u_x + w_y rho u_y),
+ * so w_x = 1 gives the x drag the fluid exerts on the porous solid,
+ * sum gamma rho u_x (the Darcy force is -gamma rho u on the fluid).  Its
+ * gamma gradient includes the explicit term. */
+lbmx_status lbmx_adjoint_set_objective_ex(lbmx_adjoint* a, const float* weights, int32_t first_step, int32_t kind);
 /* nsteps steps from the initial state; J into *objective */
 lbmx_status lbmx_adjoint_forward(lbmx_adjoint* a, int32_t nsteps, double* objective);
 /* dJ/dgamma[n] (may be NULL) and {dJ/domega, dJ/dFx, dJ/dFy} of the last forward run */

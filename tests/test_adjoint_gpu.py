@@ -3,7 +3,10 @@ respect to the Brinkman field, omega and the body force.
 
 The gradient is checked against central finite differences of the FP64
 oracle's objective (the oracle restates the same step, Brinkman term
-included) to 1e-3 relative; the adjoint's forward model against the engine;
+included) to 1e-3 relative, and against the FP64 host adjoint
+(oracle/adjoint64.py: reverse-mode gradient of an FP64 restatement of the
+oracle's step) node by node; the Brinkman-drag objective likewise; the
+adjoint's forward model against the engine;
 the checkpoint interval must not change the gradient; the autograd wrapper
 must return the adjoint's gradient.
 """
@@ -181,3 +184,72 @@ def test_adjoint_rejects_what_it_does_not_differentiate():
     zg[:, 0] = C.ZG_OUTFLOW
     with pytest.raises(lbmx.LbmxError):
         lbmx.Adjoint(NX, NY, op=C.BGK, omega=c["omega"], periodic=(True, False), flags=zg)
+
+
+def host_adjoint(c, drag=False):
+    import adjoint64 as A
+    m = A.Model(c["nx"], c["ny"], c["op"], c["S"], c["omega"], c["flags"], c["periodic"], c["rho"], c["u"],
+                weights(c), FIRST, T, drag=drag)
+    return m.gradient(c["gamma"].astype(np.float64), c["omega"], float(c["force"][0].flat[0]), 0.0)
+
+
+# FP32 gradient against the FP64 one: per scalar, and over the gamma field
+# as a whole (a component's error relative to the field's norm)
+HOST_RTOL = {C.BGK: 2e-5, C.MRT: 2e-5, C.CM: 2e-5, C.CM_OPT: 1e-4}
+
+
+@pytest.mark.parametrize("op", [C.BGK, C.MRT, C.CM, C.CM_OPT])
+@pytest.mark.parametrize("drag", [False, True])
+def test_adjoint_gradient_matches_the_fp64_host_adjoint(op, drag):
+    c = case(op)
+    a = make_adjoint(c)
+    if drag:
+        a.set_objective(weights(c), FIRST, kind=lbmx.OBJECTIVE_BRINKMAN_DRAG)
+    J = a.forward(T)
+    g, (g_om, g_fx, g_fy) = a.backward()
+    J64, g64, om64, fx64, fy64 = host_adjoint(c, drag)
+    tol = HOST_RTOL[op]
+    print("op %d drag %d: J %.9e / %.9e, omega %.6e / %.6e, Fx %.6e / %.6e, |dg|/|g| %.2e" % (
+        op, drag, J, J64, g_om, om64, g_fx, fx64, np.linalg.norm(g - g64) / np.linalg.norm(g64)))
+    assert abs(J - J64) <= 1e-6 + 1e-5 * abs(J64)
+    assert rel(g_om, om64) < tol and rel(g_fx, fx64) < tol
+    assert abs(g_fy - fy64) <= tol * (abs(fy64) + abs(fx64))
+    assert np.abs(g - g64).max() <= tol * np.linalg.norm(g64)
+    assert np.linalg.norm(g - g64) <= tol * np.linalg.norm(g64)
+
+
+def test_brinkman_drag_gradient_matches_fp64_finite_differences():
+    """The drag objective's gamma gradient, explicit term included, against
+    central differences of the FP64 oracle's drag sum gamma rho u_x."""
+    import oracle as O
+    c = case(C.MRT, gamma_scale=0.3)
+    a = make_adjoint(c)
+    a.set_objective(weights(c), FIRST, kind=lbmx.OBJECTIVE_BRINKMAN_DRAG)
+    a.forward(T)
+    g, _ = a.backward()
+    w = weights(c).astype(np.float64)
+    fx = float(c["force"][0].flat[0])
+
+    def J(gam):
+        o = O.Oracle(c["nx"], c["ny"], op=c["op"], omega=c["omega"], S=c["S"], periodic=c["periodic"],
+                     precision="f64")
+        o.set_flags(c["flags"])
+        o.set_gamma(gam)
+        F = np.zeros((2, c["ny"], c["nx"]))
+        F[0] = fx
+        o.init(c["rho"], c["u"], F)
+        tot = 0.0
+        for t in range(1, T + 1):
+            o.step(1)
+            if t >= FIRST:
+                r, u, _ = o.moments()
+                tot += float((gam * (w[0] * r + w[1] * r * u[0] + w[2] * r * u[1])).sum())
+        return tot
+
+    gam = c["gamma"].astype(np.float64)
+    for (y, x) in ((NY // 2, NX - 1), (3, NX - 1), (NY // 2, 5)):
+        e = np.zeros_like(gam)
+        e[y, x] = 1.0
+        h = 1e-6
+        fd = (J(gam + h * e) - J(gam - h * e)) / (2 * h)
+        assert abs(g[y, x] - fd) < RTOL * max(abs(fd), 1e-3 * np.abs(g).max()), (y, x, g[y, x], fd)
