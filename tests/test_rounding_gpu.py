@@ -5,7 +5,7 @@ every step, a persistent source term that the slow viscous modes amplify
 with the lattice size; stochastic rounding (the default) makes every store
 unbiased.  Checked on the lid-driven cavity at Re 1000 run towards steady
 state: against the engine's FP32 run, against the FP64 oracle's field after
-100,000 steps (tests/golden/steady_cavity256_mrt.npz, made by
+its steady state (tests/golden/steady_cavity256_mrt.npz, made by
 make_steady_cavity.py in that folder), and for bitwise reproducibility.
 """
 import os
@@ -52,14 +52,23 @@ def test_stochastic_rounding_removes_the_steady_state_bias():
 
 
 def test_steady_state_against_the_fp64_oracle():
+    """At steady state (the FP64 field changes by at most 1e-6 over its last
+    1000 steps) FP16 offset storage with stochastic rounding is as close to
+    FP64 as FP32 storage is (both about 1.1e-3: FP32 stores f itself, whose
+    rounding the slow modes amplify as well); BF16 within 1e-2."""
+    import json
     g = np.load(GOLDEN)
+    meta = json.loads(str(g["meta"]))
+    assert meta["residual_last_1000_steps"] <= 1e-6
     ref = g["u"]
     err = {}
     for storage in (F32, F16, BF16):
-        u = velocity(256, storage, 100000)
+        u = velocity(256, storage, meta["steps"])
         err[storage] = l2(u[:, ::4, ::4], ref)
-    assert err[F32] < 1e-3, err
-    assert err[F16] < 2e-3, err
+    print("steady-state L2 error vs FP64 after %d steps: FP32 %.2e FP16 %.2e BF16 %.2e"
+          % (meta["steps"], err[F32], err[F16], err[BF16]))
+    assert err[F32] < 1.5e-3, err
+    assert err[F16] < 1.2 * err[F32], err
     assert err[BF16] < 1e-2, err
 
 
