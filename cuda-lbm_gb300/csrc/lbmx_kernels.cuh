@@ -644,6 +644,8 @@ __device__ __forceinline__ void opt_terms(const StepArgs& a, long long off, cons
 // in exact fixed point, so the averages do not depend on the order.
 template <typename T>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) opt_prepass_kernel(const StepArgs a) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" :::);
     Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};
     const Geometry& g = a.g;
     const T* F = static_cast<const T*>(a.f);
@@ -707,6 +709,8 @@ __device__ __forceinline__ void edge_coords(int e, int nx, int ny, int* x, int* 
 // post-stream state before any boundary is applied.
 template <typename T>
 __global__ void edge_prepass_kernel(const StepArgs a, float* aux) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" :::);
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= a.g.perimeter) return;
     int x, y;
@@ -931,17 +935,34 @@ cudaError_t launch_step(const StepArgs& a, const CUtensorMap& tmap, int op, cuda
 #undef LBMX_STEP_CASE
 }
 
+// A launch with programmatic stream serialization: the kernel may start
+// during the previous grid's tail and waits in griddepcontrol.wait before
+// its first dependent access (the pre-passes and the IBM kernel sit between
+// two step kernels, which are launched the same way).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <typename T>
 cudaError_t launch_opt_prepass(const StepArgs& a, cudaStream_t s) {
-    // as many CTAs as the step kernel, so the FP64 partials buffer fits both
-    opt_prepass_kernel<T><<<a.num_ctas, kThreads, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(opt_prepass_kernel<T>, (unsigned)a.num_ctas, kThreads, s, a);
 }
 
 template <typename T>
 cudaError_t launch_edge_prepass(const StepArgs& a, float* aux, cudaStream_t s) {
-    edge_prepass_kernel<T><<<(a.g.perimeter + 127) / 128, 128, 0, s>>>(a, aux);
-    return cudaGetLastError();
+    return launch_pdl(edge_prepass_kernel<T>, (unsigned)((a.g.perimeter + 127) / 128), 128u, s, a, aux);
 }
 
 template <typename T>
