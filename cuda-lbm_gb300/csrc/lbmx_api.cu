@@ -101,6 +101,9 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     a.special_units = h->special_units;
     a.nspecial = h->nspecial;
     a.special_chunks = h->special_chunks;
+    a.dep_chunk = h->dep_chunk;
+    a.tile_order = h->tile_order;
+    a.dep_tile = h->dep_tile;
     a.special_bits = h->special_bits;
     a.tiles_x = h->tiles_x;
     a.tiles_y = h->tiles_y;
@@ -112,10 +115,11 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
     return a;
 }
 
-// Split the lattice between the two kinds of step-kernel CTAs: units (two
-// x-neighbouring nodes, x0 even) on the perimeter or holding a flagged or
-// IBM-forced node take the general path; the kernel finds perimeter units by
-// position and the others through a bit per unit.
+// Split the lattice between the two kinds of step-kernel work items: units
+// (two x-neighbouring nodes, x0 even) on the perimeter or holding a flagged
+// node take the general path; the kernel finds perimeter units by position
+// and the others through a bit per unit.  IBM patch nodes stay in the tiles,
+// which add the IBM force when they hold one.
 static lbmx_status rebuild_special(lbmx_handle* h) {
     const Geometry& g = h->g;
     const int units_per_row = g.pitch / 2;
@@ -129,15 +133,10 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
         for (int y = 0; y < g.ny; y++)
             for (int x = 0; x < g.nx; x++)
                 if (h->flags_host[(size_t)y * g.pitch + x]) mark((long long)y * g.pitch + x);
-    for (int off : h->patch_host) mark(off);
     // an own-node step (parity 0) runs a node through the tiles unless it has
-    // a boundary functor, an IBM patch force or (fluid on a non-periodic
-    // edge) reads the edge store
-    std::vector<char> patch((size_t)g.plane, 0);
-    for (int off : h->patch_host) patch[(size_t)off] = 1;
+    // a boundary functor or (fluid on a non-periodic edge) reads the edge store
     auto plain0 = [&](int x, int y) {
         const size_t off = (size_t)y * g.pitch + x;
-        if (patch[off]) return false;
         const uint8_t f = h->flags_host.empty() ? (uint8_t)LBMX_FLUID : h->flags_host[off];
         if (f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB) return true;
         const bool edge = (!g.periodic_x && (x == 0 || x == g.nx - 1)) || (!g.periodic_y && (y == 0 || y == g.ny - 1));
@@ -173,6 +172,35 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
                 bits0[u >> 5] |= 1u << (u & 31);
             }
         }
+    // Work that touches the IBM patch goes last: with the IBM kernel still
+    // running, the step kernel takes every other item first.  A node's update
+    // reads and writes only its own AA slots and reads its own force entry,
+    // and the IBM kernel reads the patch nodes' slots and writes their
+    // forces; the margin of one node covers boundary functors that read a
+    // neighbour.  In each list the units near the patch go last, and the
+    // tiles near it follow all others.
+    std::vector<char> near;
+    if (!h->patch_host.empty()) {
+        near.assign((size_t)g.plane, 0);
+        for (int off : h->patch_host) {
+            const int py = off / g.pitch, px = off % g.pitch;
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    int x = px + dx, y = py + dy;
+                    if (g.periodic_x) x = (x + g.nx) % g.nx;
+                    if (g.periodic_y) y = (y + g.ny) % g.ny;
+                    if (x >= 0 && x < g.nx && y >= 0 && y < g.ny) near[(size_t)y * g.pitch + x] = 1;
+                }
+        }
+    }
+    const auto by_patch = [&](std::vector<int>& list) {
+        if (near.empty()) return (int)list.size();
+        const auto it = std::stable_partition(list.begin(), list.end(), [&](int u) {
+            return !near[(size_t)u] && !(u % g.pitch + 1 < g.nx && near[(size_t)u + 1]);
+        });
+        return (int)(it - list.begin());
+    };
+    const int indep = by_patch(units), indep0 = by_patch(units0);
     cudaFree(h->special_units);
     cudaFree(h->special_bits);
     cudaFree(h->special_units0);
@@ -196,9 +224,34 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
     h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
     h->nspecial0 = (int)units0.size();
     h->special_chunks0 = (2 * h->nspecial0 + kSpecialChunk - 1) / kSpecialChunk;
+    // a chunk is dependent from the one holding the first patch-adjacent unit
+    h->dep_chunk = indep == h->nspecial ? h->special_chunks : 2 * indep / kSpecialChunk;
+    h->dep_chunk0 = indep0 == h->nspecial0 ? h->special_chunks0 : 2 * indep0 / kSpecialChunk;
     const int es = (int)elem_size(h->p.storage);
-    h->tiles_x = (g.nx + step_tile_w(es) - 1) / step_tile_w(es);
-    h->tiles_y = (g.ny + step_tile_h(es) - 1) / step_tile_h(es);
+    const int tw = step_tile_w(es), th = step_tile_h(es);
+    h->tiles_x = (g.nx + tw - 1) / tw;
+    h->tiles_y = (g.ny + th - 1) / th;
+    cudaFree(h->tile_order);
+    h->tile_order = nullptr;
+    h->dep_tile = h->tiles_x * h->tiles_y;
+    if (!near.empty()) {
+        std::vector<int> first, last;
+        for (int t = 0; t < h->tiles_x * h->tiles_y; t++) {
+            const int ty = t / h->tiles_x, tx = t % h->tiles_x;
+            bool touches = false;
+            for (int y = ty * th; y < std::min(g.ny, ty * th + th) && !touches; y++)
+                for (int x = tx * tw; x < std::min(g.nx, tx * tw + tw); x++)
+                    if (near[(size_t)y * g.pitch + x]) {
+                        touches = true;
+                        break;
+                    }
+            (touches ? last : first).push_back(t);
+        }
+        h->dep_tile = (int)first.size();
+        first.insert(first.end(), last.begin(), last.end());
+        LBMX_CUDA(h, cudaMalloc((void**)&h->tile_order, first.size() * sizeof(int)));
+        LBMX_CUDA(h, cudaMemcpy(h->tile_order, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     // persistent CTAs walk the work list: kCtasPerSm per SM on large
     // lattices; two per SM when each CTA would get fewer than 16 items (a
     // small lattice is latency-bound and gains more from fuller CTAs than
@@ -240,6 +293,7 @@ void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.special_units = a.parity ? h->special_units : h->special_units0;
     a.nspecial = a.parity ? h->nspecial : h->nspecial0;
     a.special_chunks = a.parity ? h->special_chunks : h->special_chunks0;
+    a.dep_chunk = a.parity ? h->dep_chunk : h->dep_chunk0;
     a.special_bits = a.parity ? h->special_bits : h->special_bits0;
     // two work counters, alternating by step: each launch zeroes the other
     a.tile_counter = h->tile_counter + (s & 1);
@@ -294,7 +348,7 @@ void lbmx_destroy(lbmx_handle* h) {
     cudaFree(h->force); cudaFree(h->gamma); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
     cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums); cudaFree(h->raw_sums);
     cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
-    cudaFree(h->special_units0); cudaFree(h->special_bits0);
+    cudaFree(h->special_units0); cudaFree(h->special_bits0); cudaFree(h->tile_order);
     cudaFree(h->tile_counter);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     cudaSetDevice(cur);
@@ -596,6 +650,9 @@ static lbmx_status run_step(lbmx_handle* h, bool store, bool check, bool sums, b
     }
     a.check_finite = check ? 1 : 0;
     a.series = series;
+    // with the IBM kernel just launched, the step starts on the items away
+    // from the patch while the marker rounds run
+    a.early = h->nm > 0 ? 1 : 0;
     // the previous step's sums, if it left them to this launch
     if (h->pend_acc) {
         a.pub_acc = h->pend_acc;

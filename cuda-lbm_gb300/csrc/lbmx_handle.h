@@ -60,6 +60,9 @@ struct lbmx_handle {
     int* special_units0 = nullptr;
     uint32_t* special_bits0 = nullptr;
     int nspecial0 = 0, special_chunks0 = 0;
+    int dep_chunk = 0, dep_chunk0 = 0;  // first chunk of each list with units next to the IBM patch
+    int* tile_order = nullptr;          // tiles away from the IBM patch, then the others (null without markers)
+    int dep_tile = 0;                   // tiles away from the patch
     int nspecial = 0, special_chunks = 0, tiles_x = 0, tiles_y = 0, num_ctas = 0, num_sms = 1;
     void* f_alloc = nullptr;  // population allocation including the guard elements
     unsigned long long* tile_counter = nullptr;  // [2] work counters, alternating by step

@@ -63,15 +63,27 @@ struct StepArgs {
     // work split of the step kernel (lbmx_kernels.cuh)
     // The general path's units of this step (set_step picks the parity's):
     // a neighbour-access step (parity 1) takes every perimeter unit (the
-    // tiles find them by position) and the units with a flagged or IBM-patch
-    // node (special_bits marks those off the perimeter); an own-node step
-    // (parity 0) only units with a boundary functor, an IBM patch node, a
-    // fluid node reading the edge store or a missing second node
+    // tiles find them by position) and the units with a flagged node
+    // (special_bits marks those off the perimeter); an own-node step
+    // (parity 0) only units with a boundary functor, a fluid node reading
+    // the edge store or a missing second node
     // (special_bits marks them all) -- there a half-way or moving wall node
     // reads and writes only its own slots, exactly as an interior node does.
     const int* special_units;      // unit offsets y*pitch + x0 handled by the general path
     int nspecial;
     int special_chunks;            // work items of kSpecialChunk special nodes that lead the work list
+    // chunks from dep_chunk on hold units within one node of an IBM patch
+    // node (the list puts those units last); they go after the early tiles.
+    // With the tiles below, they are the only items that read what the IBM
+    // kernel of this step writes or write what it reads.
+    // dep_chunk = special_chunks: none.
+    int dep_chunk;
+    // tiles in tile_order from dep_tile on hold a node within one node of an
+    // IBM patch node: they follow the dependent chunks and add the IBM force
+    // (tile_order null: no IBM, tiles in place)
+    const int* tile_order;
+    int dep_tile;
+    int early;                     // run the items before the dependent ones before waiting on the preceding grid
     const uint32_t* special_bits;  // 1 bit per unit (see above), or nullptr
     int tiles_x, tiles_y;          // tiles of kStageW x kStageH nodes covering the lattice
     int num_ctas;                  // persistent CTAs that walk the interior tiles

@@ -169,8 +169,10 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
         fy = a.force[a.g.plane + off];
     }
     if (a.ibm_force) {
-        fx += a.ibm_force[off];
-        fy += a.ibm_force[a.g.plane + off];
+        // written by the IBM kernel this grid may have overlapped: read
+        // through L2
+        fx += __ldcg(a.ibm_force + off);
+        fy += __ldcg(a.ibm_force + a.g.plane + off);
     }
     *Fx = fx;
     *Fy = fy;
@@ -355,7 +357,7 @@ __host__ __device__ constexpr int mode_sums(int mode) { return mode == kModeLean
 // Collide two staged interior nodes (x0, x0+1) of row y and store them in place.
 template <typename T, int OP, int P, int TW = kStageW, int TH = kStageH, int MODE = kModeFull>
 __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, int r, int lx, int x0, int y,
-                                              Acc v[kNumSums], uint32_t seed) {
+                                              Acc v[kNumSums], uint32_t seed, const float* ibf = nullptr) {
     using St = Staging<T, TW, TH>;
     const Geometry& g = a.g;
     T* F = static_cast<T*>(a.f);
@@ -380,6 +382,12 @@ __device__ __forceinline__ void interior_unit(const StepArgs& a, const T* sbuf, 
     if (MODE == kModeFull && a.force) {
         Fx.v = *reinterpret_cast<const float2*>(a.force + off);
         Fy.v = *reinterpret_cast<const float2*>(a.force + plane + off);
+    }
+    if (ibf) {
+        // a tile with IBM patch nodes: the forces this step's IBM kernel
+        // wrote (zero off the patch), through L2 as in node_force
+        Fx = Fx + V2{__ldcg(reinterpret_cast<const float2*>(ibf + off))};
+        Fy = Fy + V2{__ldcg(reinterpret_cast<const float2*>(ibf + plane + off))};
     }
     const V2 inv = vdiv(splat(1.0f, rho), rho);
     V2 ux = fma(0.5f * Fx, inv, jx * inv);
@@ -474,10 +482,10 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     constexpr int TW = step_tile_w((int)sizeof(T)), TH = step_tile_h((int)sizeof(T));
     // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
     // work item from a global counter; for an interior tile it bulk-copies
-    // the tile into the ring), warps 0-7 consume.  Items 0..special_chunks-1
+    // the tile into the ring), warps 0-7 consume.  Items 0..dep_chunk-1
     // are chunks of special nodes (general path, one node per consumer
     // thread, nothing staged) so the boundary work spreads over every SM;
-    // the interior tiles follow.  full[s] completes when a stage's bytes have
+    // the interior tiles follow, then the chunks next to an IBM patch.  full[s] completes when a stage's bytes have
     // landed (or at once for a special chunk); empty[s] when all eight
     // consumer warps are done with it.
     using St = Staging<T, TW, TH>;
@@ -489,7 +497,13 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     uint64_t* empty = full + St::NST;
     int4* slot = reinterpret_cast<int4*>(empty + St::NST);
     const int nchunks = a.special_chunks;
-    const int nitems = nchunks + a.tiles_x * a.tiles_y;
+    const int ntiles = a.tiles_x * a.tiles_y;
+    const int nitems = nchunks + ntiles;
+    // item order: chunks [0, dep), the tiles that do not wait, chunks
+    // [dep, nchunks), then the tiles that do (tile_order lists the tiles in
+    // that order; without it every tile is early and in place)
+    const int dep = min(a.dep_chunk, nchunks);
+    const int early_tiles = a.tile_order ? a.dep_tile : ntiles;
     const int warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int s = 0; s < St::NST; s++) {
@@ -504,7 +518,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     // let the next step's grid start its own prologue: every CTA of this grid
     // is resident by now, so the waiting grid cannot hold SM slots this one
     // still needs.  Without the launch attribute both are no-ops.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // `early` (the IBM kernel of this step precedes): that kernel started
+    // only after the previous step had finished, and it reads and writes
+    // only the patch nodes' slots and forces, so every item before the
+    // dependent chunks runs at once; the producer marks the dependent chunks
+    // and each thread waits before its first one, and before it exits.
+    if (!a.early) asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" :::);
     if (tid == 0 && blockIdx.x == 0) {
         // the next step's work counter (the previous launch used it and has
@@ -540,19 +559,27 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                 }
                 break;
             }
-            if (item < nchunks) {
+            int chunk = -1, tile;
+            const bool later = item >= dep + early_tiles;
+            if (item < dep) chunk = item;
+            else if (item < dep + early_tiles) tile = item - dep;
+            else if (item < nchunks + early_tiles) chunk = item - early_tiles;
+            else tile = item - nchunks;
+            if (chunk >= 0) {
                 if (lane == 0) {
-                    put_slot(&slot[s], -2 - item, 0, 0, 0);
+                    put_slot(&slot[s], -2 - chunk, 0, 0, later ? 1 : 0);
                     mbar_arrive(&full[s]);
                 }
                 __syncwarp();
                 continue;
             }
-            const int tile = item - nchunks;
+            // a tile that waits is staged at once all the same: the IBM
+            // kernel only reads populations
+            if (a.tile_order) tile = __ldg(a.tile_order + tile);
             const int ty = tile / a.tiles_x, tx = tile - ty * a.tiles_x;
             const int x0 = tx * St::TW, y0 = ty * St::TH;
             if (lane == 0) {
-                put_slot(&slot[s], tile, x0, y0, 0);
+                put_slot(&slot[s], tile, x0, y0, later ? 1 : 0);
                 fence_proxy_async_smem();
                 mbar_expect_tx(&full[s], St::STAGE_BYTES);
             }
@@ -568,6 +595,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     } else {
         // consumers
         const int lx = tid % (St::TW / 2), r0 = tid / (St::TW / 2);
+        bool waited = !a.early;
         for (int i = 0;; i++) {
             const int s = i % St::NST;
             if (!mbar_wait(&full[s], (unsigned)((i / St::NST) & 1), kWaitLimit)) {
@@ -576,9 +604,14 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
             }
             const int4 sl = get_slot(&slot[s]);
             if (sl.x == -1) break;
+            if (sl.w && !waited) {
+                asm volatile("griddepcontrol.wait;" ::: "memory");
+                waited = true;
+            }
             if (sl.x < 0) {
                 special_chunk<T, OP, MODE>(a, -2 - sl.x, tid, v, a.sr_seed);
             } else {
+                const float* ibf = sl.w ? a.ibm_force : nullptr;
                 const int x0 = sl.y + 2 * lx;
 #pragma unroll 1
                 for (int r = r0; r < TH; r += St::ROWS) {
@@ -593,13 +626,15 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                     }
                     if (live)
                         interior_unit<T, OP, P, TW, TH, MODE>(a, bufs + (size_t)s * St::STAGE_ELEMS, r, lx, x0, y,
-                                                              v, a.sr_seed);
+                                                              v, a.sr_seed, ibf);
                 }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[s]);
         }
     }
+    // an early-started grid finishes only after the grid it overlapped
+    if (a.early) asm volatile("griddepcontrol.wait;" ::: "memory");
     // kModeSums: each warp adds its totals and is done (the next launch
     // publishes them); kModeFull: the last CTA publishes
     if (MODE == kModeSums) warp_sums(a.partials, v, sums_mask(false, false));
