@@ -178,12 +178,15 @@ __device__ __forceinline__ void node_force(const StepArgs& a, long long off, flo
     *Fy = fy;
 }
 
-// One node through the general path (special units).  Kept out of line: the
-// single-lattice and the batched step kernels then run the same compiled
-// code for boundary nodes, so a lattice gets bit-identical results from both
-// (inlined, the two callers may contract multiply-adds differently).
+// One node through the general path (special units).  The lean and sums
+// step variants inline it (one node per thread is a long dependent chain;
+// the arguments then come straight from the parameter bank); the full
+// variants, whose tiles need every register, call it out of line
+// (general_node).  Both step kernels, single-lattice and batched, make the
+// same choice for the same variant, so a lattice steps bit for bit alike
+// in either.
 template <typename T, int OP>
-__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[kNumSums], uint32_t seed) {
+__device__ __forceinline__ void general_node_body(const StepArgs& a, int x, int y, Acc v[kNumSums], uint32_t seed) {
     const long long off = (long long)y * a.g.pitch + x;
     float f[9];
     unsigned outmask;
@@ -239,6 +242,11 @@ __device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v
         collide_cm<float>(f, rho, rho, ux, uy, Fx, Fy, a.S, optimal_rate<float>(rho, jmag, pimag, a.avg), true);
     }
     store_post_collision<T>(a, x, y, f, outmask, fl, seed);
+}
+
+template <typename T, int OP>
+__device__ __noinline__ void general_node(const StepArgs& a, int x, int y, Acc v[kNumSums], uint32_t seed) {
+    general_node_body<T, OP>(a, x, y, v, seed);
 }
 
 // ---------------------------------------------------------------- staging
@@ -471,7 +479,8 @@ __device__ __forceinline__ void special_chunk(const StepArgs& a, int chunk, int 
     // the out-of-line call gets its own accumulators, so the caller's stay
     // in registers
     Acc t[kNumSums] = {0, 0, 0, 0, 0, 0};
-    general_node<T, OP>(a, x, y, t, seed);
+    if (MODE == kModeFull) general_node<T, OP>(a, x, y, t, seed);
+    else general_node_body<T, OP>(a, x, y, t, seed);
     if (mode_sums(MODE) > 0 && a.partials)
 #pragma unroll
         for (int k = 0; k < mode_sums(MODE); k++) v[k] += t[k];
@@ -512,6 +521,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    // The out-of-line general path (full variants) reads the arguments
+    // through a pointer: into this shared copy, not into the kernel's
+    // parameter space, which a pointer reaches only through slow generic
+    // loads (a 256-node chunk took 1.3 times as long from there).
+    __shared__ StepArgs sa;
+    if (MODE == kModeFull && tid == 32 && nchunks > 0) sa = a;
     // Programmatic dependent launch: this grid may have started while the
     // previous step's grid was still draining.  Wait for that grid to finish
     // (its writes are then visible) before touching anything it wrote, then
@@ -609,7 +624,8 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                 waited = true;
             }
             if (sl.x < 0) {
-                special_chunk<T, OP, MODE>(a, -2 - sl.x, tid, v, a.sr_seed);
+                if (MODE == kModeFull) special_chunk<T, OP, MODE>(sa, -2 - sl.x, tid, v, a.sr_seed);
+                else special_chunk<T, OP, MODE>(a, -2 - sl.x, tid, v, a.sr_seed);
             } else {
                 const float* ibf = sl.w ? a.ibm_force : nullptr;
                 const int x0 = sl.y + 2 * lx;
