@@ -252,16 +252,23 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
         LBMX_CUDA(h, cudaMalloc((void**)&h->tile_order, first.size() * sizeof(int)));
         LBMX_CUDA(h, cudaMemcpy(h->tile_order, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
-    // persistent CTAs walk the work list: kCtasPerSm per SM on large
-    // lattices; two per SM when each CTA would get fewer than 16 items (a
-    // small lattice is latency-bound and gains more from fuller CTAs than
-    // from more warps)
-    const long long items = (long long)h->tiles_x * h->tiles_y + h->special_chunks;
-    const int per_sm = items >= 16LL * kCtasPerSm * h->num_sms ? kCtasPerSm : 2;
-    h->num_ctas = (int)std::max<long long>(1, std::min<long long>(items, (long long)per_sm * h->num_sms));
-    // claim items in chunks of about 1/16 of a CTA's share: few atomics on
-    // large lattices, still one item at a time on small ones
-    h->tile_chunk = (int)std::max<long long>(1, items / (16LL * h->num_ctas));
+    // Persistent CTAs walk the work list, kCtasPerSm per SM, except in the
+    // steps of a small lattice (fewer than 16 items per CTA) that have
+    // general-path chunks: there two per SM.  A chunk is one node per
+    // thread, a long chain of dependent loads and arithmetic that a third
+    // CTA on the SM stretches past the end of the tiles (on a 1024^2 cavity
+    // 9 -> 14 us), while without chunks the third CTA hides more of the
+    // tiles' latency (13.3 -> 11.5 us).  Claims take about 1/16 of a CTA's
+    // share: few atomics on large lattices, one item at a time on small ones.
+    const long long tiles = (long long)h->tiles_x * h->tiles_y;
+    const auto split = [&](int chunks, int* num_ctas, int* tile_chunk) {
+        const long long items = tiles + chunks;
+        const int per_sm = (items >= 16LL * kCtasPerSm * h->num_sms || chunks == 0) ? kCtasPerSm : 2;
+        *num_ctas = (int)std::max<long long>(1, std::min<long long>(items, (long long)per_sm * h->num_sms));
+        *tile_chunk = (int)std::max<long long>(1, items / (16LL * *num_ctas));
+    };
+    split(h->special_chunks, &h->num_ctas, &h->tile_chunk);
+    split(h->special_chunks0, &h->num_ctas0, &h->tile_chunk0);
     if (!h->partials) {
         // two sets (one per step parity) of kSumSlots copies of the six
         // fixed-point grid accumulators (zero between uses)
@@ -294,6 +301,8 @@ void lbmx::set_step(const lbmx_handle* h, StepArgs& a, long long s) {
     a.nspecial = a.parity ? h->nspecial : h->nspecial0;
     a.special_chunks = a.parity ? h->special_chunks : h->special_chunks0;
     a.dep_chunk = a.parity ? h->dep_chunk : h->dep_chunk0;
+    a.num_ctas = a.parity ? h->num_ctas : h->num_ctas0;
+    a.tile_chunk = a.parity ? h->tile_chunk : h->tile_chunk0;
     a.special_bits = a.parity ? h->special_bits : h->special_bits0;
     // two work counters, alternating by step: each launch zeroes the other
     a.tile_counter = h->tile_counter + (s & 1);

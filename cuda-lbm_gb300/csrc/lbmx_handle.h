@@ -69,7 +69,8 @@ struct lbmx_handle {
     long long last_step = -2;      // step index of the last single-lattice launch
     double* pend_acc = nullptr;    // accumulators of a step whose sums are not yet published
     double* pend_series = nullptr; // and that step's series entry or null
-    int tile_chunk = 1;
+    int tile_chunk = 1;            // neighbour-access steps (num_ctas, tile_chunk) and own-node
+    int num_ctas0 = 0, tile_chunk0 = 1;  // steps (num_ctas0, tile_chunk0)
     CUtensorMap tmap;  // the type carries the 64-byte alignment TMA needs  // TMA descriptor of the population planes
     long long partial_cap = 0;
     char err[512] = {0};
