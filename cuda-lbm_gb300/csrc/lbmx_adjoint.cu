@@ -201,6 +201,372 @@ __device__ __forceinline__ void adj_block_sum(double v[C], double* part, bool ad
     }
 }
 
+// ---------------------------------------------------------------- reverse
+// The node's vector-Jacobian product in reverse mode, written out by hand
+// for BGK, MRT and CM (CM_OPT keeps the forward-mode tangents below): one
+// pass over the node's values, then their adjoints in reverse order, instead
+// of 13 tangent directions pushed through the collision.  In: the node's
+// post-stream populations ps, its gamma, mu (the adjoints of its
+// post-collision populations, centred: their mean c goes through the
+// conserved mass, below) and the objective weights w of its moments.  Out:
+// lam = d/dps of (mu . pc + objective), and the node's gamma, omega and
+// body-force derivatives.
+
+// post-collision adjoints -> moment-space adjoints of CM's back transform
+// (raw moments r from central moments c by the binomial shift by +u), the
+// collision's adjoints of rho, drho, u, F and S; b_f gets the raw-moment
+// part (the populations' own adjoints through m = M f)
+__device__ __forceinline__ void vjp_cm(const float f[9], float rho, float drho, float ux, float uy, float Fx, float Fy,
+                                       const float S[9], const float mu[9], float b_f[9], float& b_rho, float& b_drho,
+                                       float& b_ux, float& b_uy, float& b_Fx, float& b_Fy, float b_S[9]) {
+    const float third = 1.0f / 3.0f;
+    // forward: raw moments, central moments, relaxed central moments
+    const float m10 = (f[1] - f[3]) + ((f[5] + f[8]) - (f[6] + f[7]));
+    const float m01 = (f[2] - f[4]) + ((f[5] + f[6]) - (f[7] + f[8]));
+    const float m22 = (f[5] + f[6]) + (f[7] + f[8]);
+    const float m20 = (f[1] + f[3]) + m22;
+    const float m02 = (f[2] + f[4]) + m22;
+    const float m11 = (f[5] + f[7]) - (f[6] + f[8]);
+    const float m21 = (f[5] + f[6]) - (f[7] + f[8]);
+    const float m12 = (f[5] + f[8]) - (f[6] + f[7]);
+    const float ux2 = ux * ux, uy2 = uy * uy, uxy = ux * uy;
+    const float k10 = m10 - ux * rho;
+    const float k01 = m01 - uy * rho;
+    const float k20 = m20 - 2.0f * ux * m10 + ux2 * rho;
+    const float k02 = m02 - 2.0f * uy * m01 + uy2 * rho;
+    const float k11 = m11 - uy * m10 - ux * m01 + uxy * rho;
+    const float k21 = m21 - 2.0f * ux * m11 - uy * m20 + ux2 * m01 + 2.0f * uxy * m10 - ux2 * uy * rho - uy * third;
+    const float k12 = m12 - 2.0f * uy * m11 - ux * m02 + uy2 * m10 + 2.0f * uxy * m01 - ux * uy2 * rho - ux * third;
+    const float k22 = m22 - 2.0f * ux * m12 - 2.0f * uy * m21 + ux2 * m02 + uy2 * m20 + 4.0f * uxy * m11 -
+                      2.0f * ux * uy2 * m10 - 2.0f * ux2 * uy * m01 + ux2 * uy2 * rho + (ux2 + uy2) * third;
+    const float ksum = k20 + k02, kdiff = k20 - k02;
+    const float c10 = (1.0f - S[1]) * k10 + (1.0f - 0.5f * S[1]) * Fx;
+    const float c01 = (1.0f - S[2]) * k01 + (1.0f - 0.5f * S[2]) * Fy;
+    const float t3 = ksum - S[3] * (ksum - (2.0f * third) * drho);
+    const float t4 = (1.0f - S[4]) * kdiff;
+    const float c11 = (1.0f - S[5]) * k11;
+    const float c21 = (1.0f - S[6]) * k21 + (1.0f - 0.5f * S[6]) * third * Fy;
+    const float c12 = (1.0f - S[7]) * k12 + (1.0f - 0.5f * S[7]) * third * Fx;
+    const float c20 = 0.5f * (t3 + t4), c02 = 0.5f * (t3 - t4), c00 = rho;
+    // reverse: populations <- raw moments (f0 = drho - r20 - r02 + r22, ...)
+    const float b_r22 = mu[0] - 0.5f * (mu[1] + mu[3] + mu[2] + mu[4]) + 0.25f * (mu[5] + mu[6] + mu[7] + mu[8]);
+    const float b_r20 = 0.5f * (mu[1] + mu[3]) - mu[0];
+    const float b_r02 = 0.5f * (mu[2] + mu[4]) - mu[0];
+    const float b_r10 = 0.5f * (mu[1] - mu[3]);
+    const float b_r01 = 0.5f * (mu[2] - mu[4]);
+    const float b_r12 = 0.5f * (mu[3] - mu[1]) + 0.25f * ((mu[5] + mu[8]) - (mu[6] + mu[7]));
+    const float b_r21 = 0.5f * (mu[4] - mu[2]) + 0.25f * ((mu[5] + mu[6]) - (mu[7] + mu[8]));
+    const float b_r11 = 0.25f * ((mu[5] + mu[7]) - (mu[6] + mu[8]));
+    b_drho += mu[0];
+    // raw moments <- central moments (shift by +u)
+    const float b_c10 = b_r10 + 2.0f * ux * b_r20 + uy * b_r11 + 2.0f * uxy * b_r21 + uy2 * b_r12 + 2.0f * ux * uy2 * b_r22;
+    const float b_c01 = b_r01 + 2.0f * uy * b_r02 + ux * b_r11 + ux2 * b_r21 + 2.0f * uxy * b_r12 + 2.0f * ux2 * uy * b_r22;
+    const float b_c20 = b_r20 + uy * b_r21 + uy2 * b_r22;
+    const float b_c02 = b_r02 + ux * b_r12 + ux2 * b_r22;
+    const float b_c11 = b_r11 + 2.0f * ux * b_r21 + 2.0f * uy * b_r12 + 4.0f * uxy * b_r22;
+    const float b_c21 = b_r21 + 2.0f * uy * b_r22;
+    const float b_c12 = b_r12 + 2.0f * ux * b_r22;
+    const float b_c22 = b_r22;
+    b_rho += ux * b_r10 + uy * b_r01 + ux2 * b_r20 + uy2 * b_r02 + uxy * b_r11 + ux2 * uy * b_r21 + ux * uy2 * b_r12 +
+             ux2 * uy2 * b_r22;
+    b_ux += c00 * b_r10 + (2.0f * c10 + 2.0f * ux * c00) * b_r20 + (c01 + uy * c00) * b_r11 +
+            (2.0f * c11 + 2.0f * ux * c01 + 2.0f * uy * c10 + 2.0f * uxy * c00) * b_r21 +
+            (c02 + 2.0f * uy * c01 + uy2 * c00 + third) * b_r12 +
+            (2.0f * c12 + 2.0f * ux * c02 + 4.0f * uy * c11 + 2.0f * uy2 * c10 + 4.0f * uxy * c01 +
+             2.0f * ux * uy2 * c00 + 2.0f * ux * third) * b_r22;
+    b_uy += c00 * b_r01 + (2.0f * c01 + 2.0f * uy * c00) * b_r02 + (c10 + ux * c00) * b_r11 +
+            (c20 + 2.0f * ux * c10 + ux2 * c00 + third) * b_r21 +
+            (2.0f * c11 + 2.0f * ux * c01 + 2.0f * uy * c10 + 2.0f * uxy * c00) * b_r12 +
+            (2.0f * c21 + 2.0f * uy * c20 + 4.0f * ux * c11 + 4.0f * uxy * c10 + 2.0f * ux2 * c01 +
+             2.0f * ux2 * uy * c00 + 2.0f * uy * third) * b_r22;
+    // central moments <- relaxation
+    const float b_t3 = 0.5f * (b_c20 + b_c02), b_t4 = 0.5f * (b_c20 - b_c02);
+    const float b_k10 = (1.0f - S[1]) * b_c10;
+    b_S[1] += -(k10 + 0.5f * Fx) * b_c10;
+    b_Fx += (1.0f - 0.5f * S[1]) * b_c10;
+    const float b_k01 = (1.0f - S[2]) * b_c01;
+    b_S[2] += -(k01 + 0.5f * Fy) * b_c01;
+    b_Fy += (1.0f - 0.5f * S[2]) * b_c01;
+    const float b_ksum = (1.0f - S[3]) * b_t3;
+    b_drho += (2.0f * third) * S[3] * b_t3;
+    b_S[3] += -(ksum - (2.0f * third) * drho) * b_t3;
+    const float b_kdiff = (1.0f - S[4]) * b_t4;
+    b_S[4] += -kdiff * b_t4;
+    const float b_k20 = b_ksum + b_kdiff, b_k02 = b_ksum - b_kdiff;
+    const float b_k11 = (1.0f - S[5]) * b_c11;
+    b_S[5] += -k11 * b_c11;
+    const float b_k21 = (1.0f - S[6]) * b_c21;
+    b_S[6] += -(k21 + (0.5f * third) * Fy) * b_c21;
+    b_Fy += (1.0f - 0.5f * S[6]) * third * b_c21;
+    const float b_k12 = (1.0f - S[7]) * b_c12;
+    b_S[7] += -(k12 + (0.5f * third) * Fx) * b_c12;
+    b_Fx += (1.0f - 0.5f * S[7]) * third * b_c12;
+    const float b_k22 = (1.0f - S[8]) * b_c22;
+    b_drho += (third * third) * S[8] * b_c22;
+    b_S[8] += -(k22 - (third * third) * drho) * b_c22;
+    // raw moments <- central moments (shift by -u)
+    const float b_m10 = b_k10 - 2.0f * ux * b_k20 - uy * b_k11 + 2.0f * uxy * b_k21 + uy2 * b_k12 - 2.0f * ux * uy2 * b_k22;
+    const float b_m01 = b_k01 - 2.0f * uy * b_k02 - ux * b_k11 + ux2 * b_k21 + 2.0f * uxy * b_k12 - 2.0f * ux2 * uy * b_k22;
+    const float b_m20 = b_k20 - uy * b_k21 + uy2 * b_k22;
+    const float b_m02 = b_k02 - ux * b_k12 + ux2 * b_k22;
+    const float b_m11 = b_k11 - 2.0f * ux * b_k21 - 2.0f * uy * b_k12 + 4.0f * uxy * b_k22;
+    const float b_m21 = b_k21 - 2.0f * uy * b_k22;
+    const float b_m12 = b_k12 - 2.0f * ux * b_k22;
+    const float b_m22 = b_k22 + b_m20 + b_m02;
+    b_rho += -ux * b_k10 - uy * b_k01 + ux2 * b_k20 + uy2 * b_k02 + uxy * b_k11 - ux2 * uy * b_k21 -
+             ux * uy2 * b_k12 + ux2 * uy2 * b_k22;
+    b_ux += -rho * b_k10 + (2.0f * ux * rho - 2.0f * m10) * b_k20 + (uy * rho - m01) * b_k11 +
+            (2.0f * ux * m01 + 2.0f * uy * m10 - 2.0f * m11 - 2.0f * uxy * rho) * b_k21 +
+            (2.0f * uy * m01 - m02 - uy2 * rho - third) * b_k12 +
+            (2.0f * ux * m02 + 4.0f * uy * m11 - 2.0f * m12 - 2.0f * uy2 * m10 - 4.0f * uxy * m01 +
+             2.0f * ux * uy2 * rho + 2.0f * ux * third) * b_k22;
+    b_uy += -rho * b_k01 + (2.0f * uy * rho - 2.0f * m01) * b_k02 + (ux * rho - m10) * b_k11 +
+            (2.0f * ux * m10 - m20 - ux2 * rho - third) * b_k21 +
+            (2.0f * uy * m10 + 2.0f * ux * m01 - 2.0f * m11 - 2.0f * uxy * rho) * b_k12 +
+            (2.0f * uy * m20 + 4.0f * ux * m11 - 2.0f * m21 - 4.0f * uxy * m10 - 2.0f * ux2 * m01 +
+             2.0f * ux2 * uy * rho + 2.0f * uy * third) * b_k22;
+    // populations <- raw moments
+    b_f[1] += b_m10 + b_m20;
+    b_f[3] += b_m20 - b_m10;
+    b_f[2] += b_m01 + b_m02;
+    b_f[4] += b_m02 - b_m01;
+    b_f[5] += b_m22 + b_m10 + b_m01 + b_m11 + b_m21 + b_m12;
+    b_f[6] += b_m22 - b_m10 + b_m01 - b_m11 + b_m21 - b_m12;
+    b_f[7] += b_m22 - b_m10 - b_m01 + b_m11 - b_m21 - b_m12;
+    b_f[8] += b_m22 + b_m10 - b_m01 - b_m11 - b_m21 + b_m12;
+}
+
+// MRT (Lallemand-Luo basis, offset form, forced): as vjp_cm
+__device__ __forceinline__ void vjp_mrt(const float f[9], float rho, float drho, float ux, float uy, float Fx, float Fy,
+                                        const float S[9], bool quirk, const float mu[9], float b_f[9], float& b_rho,
+                                        float& b_drho, float& b_ux, float& b_uy, float& b_Fx, float& b_Fy,
+                                        float b_S[9]) {
+    const float inv_norm[9] = {1.0f / 9.0f, 1.0f / 36.0f, 1.0f / 36.0f, 1.0f / 6.0f, 1.0f / 12.0f,
+                               1.0f / 6.0f, 1.0f / 12.0f, 0.25f, 0.25f};
+    // forward: moments, equilibrium moments, force moments
+    const float axis = (f[1] + f[2]) + (f[3] + f[4]);
+    const float diag = (f[5] + f[6]) + (f[7] + f[8]);
+    const float d13 = f[1] - f[3], d24 = f[2] - f[4];
+    const float d58 = f[5] + f[8], d67 = f[6] + f[7];
+    const float d56 = f[5] + f[6], d78 = f[7] + f[8];
+    float m[9], meq[9], Fm[9];
+    m[1] = 2.0f * diag - 4.0f * f[0] - axis;
+    m[2] = 4.0f * f[0] - 2.0f * axis + diag;
+    m[3] = d13 + (d58 - d67);
+    m[4] = -2.0f * d13 + (d58 - d67);
+    m[5] = d24 + (d56 - d78);
+    m[6] = -2.0f * d24 + (d56 - d78);
+    m[7] = (f[1] + f[3]) - (f[2] + f[4]);
+    m[8] = (f[5] + f[7]) - (f[6] + f[8]);
+    const float uu = ux * ux + uy * uy;
+    const float rux = rho * ux, ruy = rho * uy;
+    meq[1] = 3.0f * rho * uu - 2.0f * drho;
+    meq[2] = drho - 3.0f * rho * uu;
+    meq[3] = rux;
+    meq[4] = -rux;
+    meq[5] = ruy;
+    meq[6] = -ruy;
+    meq[7] = rho * (ux * ux - uy * uy);
+    meq[8] = rux * uy;
+    const float fu = Fx * ux + Fy * uy;
+    Fm[1] = 6.0f * fu;
+    Fm[2] = -6.0f * fu;
+    Fm[3] = Fx;
+    Fm[4] = quirk ? Fy : -Fx;
+    Fm[5] = quirk ? -Fx : Fy;
+    Fm[6] = -Fy;
+    Fm[7] = 2.0f * (Fx * ux - Fy * uy);
+    Fm[8] = Fx * uy + Fy * ux;
+    // reverse: populations <- scaled post-collision moments a
+    float b_a[9];
+    const float b_axis_out = (mu[1] + mu[3]) + (mu[2] + mu[4]);
+    const float b_diag_out = (mu[5] + mu[6]) + (mu[7] + mu[8]);
+    const float b_ax = mu[1] - mu[3], b_ay = mu[2] - mu[4];
+    const float b_px = (mu[5] + mu[8]) - (mu[6] + mu[7]), b_py = (mu[5] + mu[6]) - (mu[7] + mu[8]);
+    b_a[0] = mu[0] + b_axis_out + b_diag_out;
+    b_a[1] = -4.0f * mu[0] - b_axis_out + 2.0f * b_diag_out;
+    b_a[2] = 4.0f * mu[0] - 2.0f * b_axis_out + b_diag_out;
+    b_a[3] = b_ax + b_px;
+    b_a[4] = b_px - 2.0f * b_ax;
+    b_a[5] = b_ay + b_py;
+    b_a[6] = b_py - 2.0f * b_ay;
+    b_a[7] = (mu[1] + mu[3]) - (mu[2] + mu[4]);
+    b_a[8] = (mu[5] + mu[7]) - (mu[6] + mu[8]);
+    b_drho += b_a[0] * (1.0f / 9.0f);
+    // a_k = inv_k ((1 - S_k) m_k + S_k meq_k + (1 - S_k / 2) Fm_k)
+    float b_m[9], b_meq[9], b_Fm[9];
+#pragma unroll
+    for (int k = 1; k < 9; k++) {
+        const float b = inv_norm[k] * b_a[k];
+        b_m[k] = (1.0f - S[k]) * b;
+        b_meq[k] = S[k] * b;
+        b_Fm[k] = (1.0f - 0.5f * S[k]) * b;
+        b_S[k] += (meq[k] - m[k] - 0.5f * Fm[k]) * b;
+    }
+    // force moments
+    const float b_fu = 6.0f * (b_Fm[1] - b_Fm[2]);
+    b_Fx += ux * b_fu + b_Fm[3] + 2.0f * ux * b_Fm[7] + uy * b_Fm[8];
+    b_Fy += uy * b_fu - b_Fm[6] - 2.0f * uy * b_Fm[7] + ux * b_Fm[8];
+    if (quirk) {
+        b_Fy += b_Fm[4];
+        b_Fx -= b_Fm[5];
+    } else {
+        b_Fx -= b_Fm[4];
+        b_Fy += b_Fm[5];
+    }
+    b_ux += Fx * b_fu + 2.0f * Fx * b_Fm[7] + Fy * b_Fm[8];
+    b_uy += Fy * b_fu - 2.0f * Fy * b_Fm[7] + Fx * b_Fm[8];
+    // equilibrium moments
+    const float b_uu = 3.0f * rho * (b_meq[1] - b_meq[2]);
+    b_rho += 3.0f * uu * (b_meq[1] - b_meq[2]) + (ux * ux - uy * uy) * b_meq[7];
+    b_drho += b_meq[2] - 2.0f * b_meq[1];
+    const float b_rux = b_meq[3] - b_meq[4] + uy * b_meq[8];
+    const float b_ruy = b_meq[5] - b_meq[6];
+    b_uy += rux * b_meq[8];
+    b_ux += 2.0f * rho * ux * b_meq[7] + rho * b_rux + 2.0f * ux * b_uu;
+    b_uy += -2.0f * rho * uy * b_meq[7] + rho * b_ruy + 2.0f * uy * b_uu;
+    b_rho += ux * b_rux + uy * b_ruy;
+    // populations <- moments
+    const float b_axis = -b_m[1] - 2.0f * b_m[2], b_diag = 2.0f * b_m[1] + b_m[2];
+    const float b_d13 = b_m[3] - 2.0f * b_m[4], b_d5867 = b_m[3] + b_m[4];
+    const float b_d24 = b_m[5] - 2.0f * b_m[6], b_d5678 = b_m[5] + b_m[6];
+    b_f[0] += 4.0f * (b_m[2] - b_m[1]);
+    b_f[1] += b_axis + b_d13 + b_m[7];
+    b_f[3] += b_axis - b_d13 + b_m[7];
+    b_f[2] += b_axis + b_d24 - b_m[7];
+    b_f[4] += b_axis - b_d24 - b_m[7];
+    b_f[5] += b_diag + b_d5867 + b_d5678 + b_m[8];
+    b_f[6] += b_diag - b_d5867 + b_d5678 - b_m[8];
+    b_f[7] += b_diag - b_d5867 - b_d5678 + b_m[8];
+    b_f[8] += b_diag + b_d5867 - b_d5678 - b_m[8];
+}
+
+// BGK (offset form, forced): as vjp_cm; b_om the omega adjoint
+__device__ __forceinline__ void vjp_bgk(const float f[9], float rho, float drho, float ux, float uy, float Fx, float Fy,
+                                        float omega, const float mu[9], float b_f[9], float& b_rho, float& b_drho,
+                                        float& b_ux, float& b_uy, float& b_Fx, float& b_Fy, float& b_om) {
+    const float uu = ux * ux + uy * uy;
+    const float pref = 1.0f - 0.5f * omega;
+    float b_uu = 0.0f, b_pref = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        const float cx = (float)CX(q), cy = (float)CY(q);
+        const float cu = cx * ux + cy * uy;
+        const float brm1 = cu * (4.5f * cu + 3.0f) - 1.5f * uu;
+        const float feq = WQ(q) * (rho * brm1 + drho);
+        const float gx = 9.0f * cx * cu + 3.0f * (cx - ux);
+        const float gy = 9.0f * cy * cu + 3.0f * (cy - uy);
+        // fn = f + omega (feq - f) + w pref (gx Fx + gy Fy)
+        const float m = mu[q];
+        b_f[q] += (1.0f - omega) * m;
+        b_om += (feq - f[q]) * m;
+        b_pref += WQ(q) * (gx * Fx + gy * Fy) * m;
+        const float b_gx = WQ(q) * pref * Fx * m, b_gy = WQ(q) * pref * Fy * m;
+        b_Fx += WQ(q) * pref * gx * m;
+        b_Fy += WQ(q) * pref * gy * m;
+        const float b_feq = omega * m;
+        b_rho += WQ(q) * brm1 * b_feq;
+        b_drho += WQ(q) * b_feq;
+        const float b_brm1 = WQ(q) * rho * b_feq;
+        const float b_cu = (9.0f * cu + 3.0f) * b_brm1 + 9.0f * (cx * b_gx + cy * b_gy);
+        b_uu += -1.5f * b_brm1;
+        b_ux += cx * b_cu - 3.0f * b_gx;
+        b_uy += cy * b_cu - 3.0f * b_gy;
+    }
+    b_om += -0.5f * b_pref;
+    b_ux += 2.0f * ux * b_uu;
+    b_uy += 2.0f * uy * b_uu;
+}
+
+// The whole node: bounce-back, macroscopics with the Guo and Brinkman
+// corrections, collision, objective.  lam[q] = d/dps_q; the parameter
+// derivatives are returned through d_gamma, d_omega, d_fx, d_fy.
+template <int OP>
+__device__ __forceinline__ void adj_node_vjp(const AdjArgs& a, int x, int y, uint8_t fl, const float ps[9], float gm,
+                                             const float mu[9], float c, const float w[3], float lam[9],
+                                             float* d_gamma, float* d_omega, float* d_fx, float* d_fy) {
+    float f[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) f[q] = ps[q];
+    adj_bc<float>(a.g, f, x, y, fl);
+    // macroscopics (adj_macro)
+    float drho = f[0], jx = 0.0f, jy = 0.0f;
+#pragma unroll
+    for (int q = 1; q < 9; q++) {
+        drho += f[q];
+        if (CX(q) == 1) jx += f[q];
+        if (CX(q) == -1) jx -= f[q];
+        if (CY(q) == 1) jy += f[q];
+        if (CY(q) == -1) jy -= f[q];
+    }
+    const float rho = drho + 1.0f;
+    const float ux0 = (jx + 0.5f * a.fx) / rho, uy0 = (jy + 0.5f * a.fy) / rho;
+    const float sc = 1.0f / (0.5f * gm + 1.0f);
+    const float ux = ux0 * sc, uy = uy0 * sc;
+    const float Fx = a.fx - gm * rho * ux, Fy = a.fy - gm * rho * uy;
+    // adjoints
+    float b_f[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float b_S[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float b_rho = 0.f, b_drho = 0.f, b_ux = 0.f, b_uy = 0.f, b_Fx = 0.f, b_Fy = 0.f, b_om = 0.f, b_gm = 0.f;
+    // objective: w0 rho + w1 rho ux + w2 rho uy (drag: times gamma)
+    {
+        const float gscale = a.drag ? gm : 1.0f;
+        b_rho += gscale * (w[0] + w[1] * ux + w[2] * uy);
+        b_ux += gscale * w[1] * rho;
+        b_uy += gscale * w[2] * rho;
+        if (a.drag) b_gm += w[0] * rho + w[1] * rho * ux + w[2] * rho * uy;
+    }
+    if (OP == LBMX_BGK)
+        vjp_bgk(f, rho, drho, ux, uy, Fx, Fy, a.omega, mu, b_f, b_rho, b_drho, b_ux, b_uy, b_Fx, b_Fy, b_om);
+    else if (OP == LBMX_MRT)
+        vjp_mrt(f, rho, drho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, mu, b_f, b_rho, b_drho,
+                b_ux, b_uy, b_Fx, b_Fy, b_S);
+    else
+        vjp_cm(f, rho, drho, ux, uy, Fx, Fy, a.S, mu, b_f, b_rho, b_drho, b_ux, b_uy, b_Fx, b_Fy, b_S);
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+        if ((a.omega_mask >> k) & 1u) b_om += b_S[k];
+    // Brinkman: F = F0 - gamma rho u, u = sc u0
+    float b_fx = b_Fx, b_fy = b_Fy;
+    b_gm += -rho * (ux * b_Fx + uy * b_Fy);
+    b_rho += -gm * (ux * b_Fx + uy * b_Fy);
+    b_ux += -gm * rho * b_Fx;
+    b_uy += -gm * rho * b_Fy;
+    const float b_ux0 = sc * b_ux, b_uy0 = sc * b_uy;
+    b_gm += -0.5f * sc * sc * (ux0 * b_ux + uy0 * b_uy);
+    // Guo correction: u0 = (j + F0 / 2) / rho
+    const float b_jx = b_ux0 / rho, b_jy = b_uy0 / rho;
+    b_fx += 0.5f * b_jx;
+    b_fy += 0.5f * b_jy;
+    b_rho += -(ux0 * b_jx + uy0 * b_jy);
+    b_drho += b_rho;
+#pragma unroll
+    for (int q = 0; q < 9; q++) b_f[q] += b_drho + (float)CX(q) * b_jx + (float)CY(q) * b_jy;
+    // bounce-back: f[OPP i] = f[i] for the links leaving the domain, undone
+    // in reverse order; the mean c of the post-collision adjoints goes
+    // through the conserved mass, whose derivative is the number of copies
+    // of each post-stream population
+    float cnt[9] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+    if (fl == LBMX_BOUNCE_BACK) {
+#pragma unroll
+        for (int i = 8; i >= 1; i--) {
+            const int xn = x + CX(i), yn = y + CY(i);
+            if (xn < 0 || xn >= a.g.nx || yn < 0 || yn >= a.g.ny) {
+                b_f[i] += b_f[OPP(i)];
+                b_f[OPP(i)] = 0.0f;
+                cnt[i] += cnt[OPP(i)];
+                cnt[OPP(i)] = 0.0f;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; q++) lam[q] = fmaf(c, cnt[q], b_f[q]);
+    *d_gamma = b_gm;
+    *d_omega = b_om;
+    *d_fx = b_fx;
+    *d_fy = b_fy;
+}
+
 __global__ void adj_init_kernel(AdjGeom g, const float* rho, const float* u, float* pc) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
@@ -306,6 +672,9 @@ __global__ void __launch_bounds__(kAdjBlock, kAdjReverseBlocksPerSm) adj_reverse
         }
         const float gm = a.gamma ? a.gamma[node] : 0.0f;
         float s[D];
+        if (OP != LBMX_CM_OPT) {
+            adj_node_vjp<OP>(a, x, y, fl, ps, gm, mu, c, w, s, &s[9], &s[10], &s[11], &s[12]);
+        } else {
         using R = Dual<kTan>;
 #pragma unroll 1
         for (int p0 = 0; p0 < D; p0 += kTan) {
@@ -349,6 +718,7 @@ __global__ void __launch_bounds__(kAdjBlock, kAdjReverseBlocksPerSm) adj_reverse
                 if (p0 + k < 9) t = fmaf(c, rintf(tsum), t);
                 s[p0 + k] = t;
             }
+        }
         }
 #pragma unroll
         for (int q = 0; q < 9; q++) lam_out[q * n + node] = s[q];
