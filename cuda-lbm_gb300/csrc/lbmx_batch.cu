@@ -121,8 +121,7 @@ static lbmx_status refresh(lbmx_batch* b) {
     if (!b->d_args) BATCH_CUDA(b, cudaMalloc((void**)&b->d_args, args.size() * sizeof(StepArgs)));
     BATCH_CUDA(b, cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(StepArgs), cudaMemcpyHostToDevice,
                                   b->stream));
-    // TMA descriptors and, per parity, the work list: special chunks of every
-    // lattice first (slower per unit), then each lattice's tiles
+    // TMA descriptors and, per parity, the work list
     std::vector<CUtensorMap> maps(n);
     for (int l = 0; l < n; l++)
         if (!encode_population_map(b->lat[l], &maps[l], tw, th))
@@ -130,17 +129,19 @@ static lbmx_status refresh(lbmx_batch* b) {
     if (!b->d_tmaps) BATCH_CUDA(b, cudaMalloc((void**)&b->d_tmaps, (size_t)n * sizeof(CUtensorMap)));
     BATCH_CUDA(b, cudaMemcpyAsync(b->d_tmaps, maps.data(), (size_t)n * sizeof(CUtensorMap), cudaMemcpyHostToDevice,
                                   b->stream));
+    // Per parity, each lattice's tiles, then its special chunks: a chunk is
+    // one node per thread, a chain of scattered loads that its lattice's
+    // tiles have just brought into L2, and the chunks spread over the whole
+    // launch instead of all waiting on DRAM together at its start.
     std::vector<int2> items[2];
     for (int p = 0; p < 2; p++) {
-        for (int l = 0; l < n; l++) {
-            const int ns = p ? b->lat[l]->nspecial : b->lat[l]->nspecial0;
-            const int chunks = (2 * ns + kSpecialChunk - 1) / kSpecialChunk;
-            for (int c = 0; c < chunks; c++) items[p].push_back(make_int2(l, -(c + 1)));
-        }
         for (int l = 0; l < n; l++) {
             const StepArgs& a = args[l];
             const long long tiles = (long long)a.tiles_x * a.tiles_y;
             for (long long t = 0; t < tiles; t++) items[p].push_back(make_int2(l, (int)t));
+            const int ns = p ? b->lat[l]->nspecial : b->lat[l]->nspecial0;
+            const int chunks = (2 * ns + kSpecialChunk - 1) / kSpecialChunk;
+            for (int c = 0; c < chunks; c++) items[p].push_back(make_int2(l, -(c + 1)));
         }
         if (items[p].size() > (size_t)0x7fffffff)
             return bfail(b, LBMX_ERR_TOO_LARGE, "lbmx_batch: too many work items");
