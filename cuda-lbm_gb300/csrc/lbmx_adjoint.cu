@@ -36,13 +36,12 @@
 namespace lbmx {
 namespace {
 
-// Threads per block of every adjoint kernel.  The reverse kernel holds a
-// node's tangents in about 140 registers; 128-thread blocks bounded to four
-// per SM (at most 128 registers, no spills for CM) keep 16 warps resident
-// where 256-thread blocks fit one per SM (8 warps): the backward pass of the
-// 2048 x 512 Brinkman channel went from 444 to 303 ms.
+// Threads per block of every adjoint kernel.  The reverse kernel's
+// tangents (CM_OPT) take about 120 registers: 128-thread blocks bounded to
+// four per SM keep 16 warps resident.  The hand-written reverse mode of the
+// other operators takes at most 110: five blocks per SM (at most 102).
 constexpr int kAdjBlock = 128;
-constexpr int kAdjReverseBlocksPerSm = 4;
+__host__ __device__ constexpr int adj_reverse_blocks_per_sm(int op) { return op == LBMX_CM_OPT ? 4 : 5; }
 constexpr int kTan = 2;  // tangents per pass
 
 struct AdjGeom {
@@ -178,17 +177,20 @@ __device__ __forceinline__ void adj_avg_terms(const R f[9], R gm, R Fx, R Fy, R 
     out[2] = adj_pimag<R>(f);
 }
 
-// deterministic block sums of C values; part[block][C] = (or +=) the sum
-template <int C>
-__device__ __forceinline__ void adj_block_sum(double v[C], double* part, bool add) {
+// deterministic block sums of C values; part[block][C] = (or +=) the sum:
+// a fixed shuffle tree within each warp in the values' type (the reverse
+// kernel's per-node gradient terms in FP32: the 64-bit pipe is narrow), the
+// warps' totals in FP64
+template <int C, typename V>
+__device__ __forceinline__ void adj_block_sum(const V v[C], double* part, bool add) {
     __shared__ double sh[kAdjBlock / 32][C];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int c = 0; c < C; c++) {
-        double t = v[c];
+        V t = v[c];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) sh[warp][c] = t;
+        if (lane == 0) sh[warp][c] = (double)t;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -592,7 +594,7 @@ __global__ void adj_avg_kernel(const AdjArgs a, const float* pc_prev, double* pa
         v[1] = t[1];
         v[2] = t[2];
     }
-    adj_block_sum<3>(v, part, false);
+    adj_block_sum<3, double>(v, part, false);
 }
 
 // one step forward; the objective terms accumulate per node when `objective`
@@ -628,13 +630,13 @@ __global__ void adj_forward_kernel(const AdjArgs a, const float* pc_prev, float*
 // writes lambda_t; g_gamma[node] += dJ/dgamma; part[block] += (domega, dFx,
 // dFy); CM_OPT: avg_part[block] = this step's sensitivity to the averages.
 template <int OP>
-__global__ void __launch_bounds__(kAdjBlock, kAdjReverseBlocksPerSm) adj_reverse_kernel(const AdjArgs a, const float* pc_prev,
+__global__ void __launch_bounds__(kAdjBlock, adj_reverse_blocks_per_sm(OP)) adj_reverse_kernel(const AdjArgs a, const float* pc_prev,
                                                                 const float* lam_next, float* lam_out,
                                                                 const float* avg, int objective, double* g_gamma,
                                                                 double* part, double* avg_part) {
     constexpr int D = OP == LBMX_CM_OPT ? 16 : 13;  // ps[9], gamma, omega, Fx, Fy [, averages]
     const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double sums[3] = {0.0, 0.0, 0.0}, asums[3] = {0.0, 0.0, 0.0};
+    float sums[3] = {0.f, 0.f, 0.f}, asums[3] = {0.f, 0.f, 0.f};
     if (node < a.g.n) {
         const long long n = a.g.n;
         const int y = (int)(node / a.g.nx), x = (int)(node - (long long)y * a.g.nx);
@@ -732,10 +734,10 @@ __global__ void __launch_bounds__(kAdjBlock, kAdjReverseBlocksPerSm) adj_reverse
             asums[2] = s[15 % D];
         }
     }
-    adj_block_sum<3>(sums, part, true);
+    adj_block_sum<3, float>(sums, part, true);
     if (OP == LBMX_CM_OPT) {
         __syncthreads();
-        adj_block_sum<3>(asums, avg_part, false);
+        adj_block_sum<3, float>(asums, avg_part, false);
     }
 }
 
