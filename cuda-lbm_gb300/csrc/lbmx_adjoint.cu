@@ -17,11 +17,12 @@
 //   mu[q]  = lambda_{t+1}[x + c_q][q]  (the half-way reflection for links
 //            that leave a wall node; 0 for links that leave the domain)
 //   lambda_t[x][i] = sum_q mu[q] dpc_q/dps_i + sum_m w_m dmoment_m/dps_i
-// with the Jacobian columns from forward-mode tangents (lbmx_dual.cuh)
-// through B and N -- the same templated device code as the forward step --
-// and the parameter gradients from the tangents of gamma, omega and F.
-// CM_OPT's rate depends on grid averages of the step; their sensitivity is
-// reduced over the grid and returned to every node in a second pass.
+// by reverse mode written out by hand through B and N (adj_node_vjp: one
+// pass over the node's values, then their adjoints in reverse order), with
+// the parameter gradients of gamma, omega and F.  CM_OPT's rate depends on
+// grid averages of the step; their sensitivity is reduced over the grid and
+// returned to every node in a second pass (forward-mode tangents,
+// lbmx_dual.cuh, of the averages' terms).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,12 +37,10 @@
 namespace lbmx {
 namespace {
 
-// Threads per block of every adjoint kernel.  The reverse kernel's
-// tangents (CM_OPT) take about 120 registers: 128-thread blocks bounded to
-// four per SM keep 16 warps resident.  The hand-written reverse mode of the
-// other operators takes at most 110: five blocks per SM (at most 102).
+// Threads per block of every adjoint kernel; the reverse kernel (about 100
+// registers) is bounded to five 128-thread blocks per SM.
 constexpr int kAdjBlock = 128;
-__host__ __device__ constexpr int adj_reverse_blocks_per_sm(int op) { return op == LBMX_CM_OPT ? 4 : 5; }
+constexpr int kAdjReverseBlocksPerSm = 5;
 constexpr int kTan = 2;  // tangents per pass
 
 struct AdjGeom {
@@ -205,9 +204,9 @@ __device__ __forceinline__ void adj_block_sum(const V v[C], double* part, bool a
 
 // ---------------------------------------------------------------- reverse
 // The node's vector-Jacobian product in reverse mode, written out by hand
-// for BGK, MRT and CM (CM_OPT keeps the forward-mode tangents below): one
-// pass over the node's values, then their adjoints in reverse order, instead
-// of 13 tangent directions pushed through the collision.  In: the node's
+// for BGK, MRT, CM and CM_OPT: one pass over the node's values, then their
+// adjoints in reverse order (forward-mode tangents pushed 13 or 16
+// directions through the collision, two at a time, 2.5 to 3 times slower).  In: the node's
 // post-stream populations ps, its gamma, mu (the adjoints of its
 // post-collision populations, centred: their mean c goes through the
 // conserved mass, below) and the objective weights w of its moments.  Out:
@@ -482,11 +481,14 @@ __device__ __forceinline__ void vjp_bgk(const float f[9], float rho, float drho,
 
 // The whole node: bounce-back, macroscopics with the Guo and Brinkman
 // corrections, collision, objective.  lam[q] = d/dps_q; the parameter
-// derivatives are returned through d_gamma, d_omega, d_fx, d_fy.
+// derivatives are returned through d_gamma, d_omega, d_fx, d_fy, and for
+// CM_OPT the derivatives of the node's term by the three grid averages
+// through d_avg.
 template <int OP>
 __device__ __forceinline__ void adj_node_vjp(const AdjArgs& a, int x, int y, uint8_t fl, const float ps[9], float gm,
-                                             const float mu[9], float c, const float w[3], float lam[9],
-                                             float* d_gamma, float* d_omega, float* d_fx, float* d_fy) {
+                                             const float mu[9], float c, const float w[3], const float* avg,
+                                             float lam[9], float* d_gamma, float* d_omega, float* d_fx, float* d_fy,
+                                             float d_avg[3]) {
     float f[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) f[q] = ps[q];
@@ -518,13 +520,59 @@ __device__ __forceinline__ void adj_node_vjp(const AdjArgs& a, int x, int y, uin
         b_uy += gscale * w[2] * rho;
         if (a.drag) b_gm += w[0] * rho + w[1] * rho * ux + w[2] * rho * uy;
     }
-    if (OP == LBMX_BGK)
+    if (OP == LBMX_BGK) {
         vjp_bgk(f, rho, drho, ux, uy, Fx, Fy, a.omega, mu, b_f, b_rho, b_drho, b_ux, b_uy, b_Fx, b_Fy, b_om);
-    else if (OP == LBMX_MRT)
+    } else if (OP == LBMX_MRT) {
         vjp_mrt(f, rho, drho, ux, uy, Fx, Fy, a.S, (a.quirks & LBMX_QUIRK_MRT_FORCE) != 0, mu, b_f, b_rho, b_drho,
                 b_ux, b_uy, b_Fx, b_Fy, b_S);
-    else
+    } else if (OP == LBMX_CM) {
         vjp_cm(f, rho, drho, ux, uy, Fx, Fy, a.S, mu, b_f, b_rho, b_drho, b_ux, b_uy, b_Fx, b_Fy, b_S);
+    } else {
+        // CM_OPT: the higher-order rate hor = 1 / (3 ts + 1/2), ts the
+        // clamped regression in rho, |j| = rho |u| and |Pi| over the grid
+        // averages (optimal_rate), in place of S[6..8]
+        const float d = (((f[5] + f[6]) + f[7]) + f[8]) + 1.0f / 3.0f;
+        const float pxx = (f[1] + f[3]) + d, pyy = (f[2] + f[4]) + d;
+        const float pxy = ((f[5] - f[6]) + f[7]) - f[8];
+        const float pimag = sqrtf(pxx * pxx + 2.0f * pxy * pxy + pyy * pyy);
+        const float umag = sqrtf(ux * ux + uy * uy);
+        const float jmag = umag * rho;
+        const float k0 = 0.0003f / avg[0], k1 = -0.00775f / avg[1], k2 = 0.00016f / avg[2];
+        const float ts0 = k0 * rho + k1 * jmag + k2 * pimag + 0.0087f;
+        const bool free = ts0 > 0.0f && ts0 <= 1.5f;  // else a constant
+        const float ts = ts0 > 0.0f ? fminf(ts0, 1.5f) : 0.005f;
+        const float hor = 1.0f / (3.0f * ts + 0.5f);
+        float Sh[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Sh[k] = k >= 6 ? hor : a.S[k];
+        vjp_cm(f, rho, drho, ux, uy, Fx, Fy, Sh, mu, b_f, b_rho, b_drho, b_ux, b_uy, b_Fx, b_Fy, b_S);
+        const float b_hor = b_S[6] + b_S[7] + b_S[8];
+        b_S[6] = b_S[7] = b_S[8] = 0.0f;
+        const float b_ts = free ? -3.0f * hor * hor * b_hor : 0.0f;
+        d_avg[0] = -k0 / avg[0] * rho * b_ts;
+        d_avg[1] = -k1 / avg[1] * jmag * b_ts;
+        d_avg[2] = -k2 / avg[2] * pimag * b_ts;
+        b_rho += k0 * b_ts + umag * k1 * b_ts;
+        const float b_umag = rho * k1 * b_ts;
+        if (umag > 0.0f) {
+            b_ux += ux / umag * b_umag;
+            b_uy += uy / umag * b_umag;
+        }
+        const float b_pimag = k2 * b_ts;
+        if (pimag > 0.0f) {
+            const float bxx = pxx / pimag * b_pimag, byy = pyy / pimag * b_pimag;
+            const float bxy = 2.0f * pxy / pimag * b_pimag;
+            const float bd = bxx + byy;
+            b_f[1] += bxx;
+            b_f[3] += bxx;
+            b_f[2] += byy;
+            b_f[4] += byy;
+            b_f[5] += bd + bxy;
+            b_f[6] += bd - bxy;
+            b_f[7] += bd + bxy;
+            b_f[8] += bd - bxy;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < 9; k++)
         if ((a.omega_mask >> k) & 1u) b_om += b_S[k];
@@ -630,11 +678,10 @@ __global__ void adj_forward_kernel(const AdjArgs a, const float* pc_prev, float*
 // writes lambda_t; g_gamma[node] += dJ/dgamma; part[block] += (domega, dFx,
 // dFy); CM_OPT: avg_part[block] = this step's sensitivity to the averages.
 template <int OP>
-__global__ void __launch_bounds__(kAdjBlock, adj_reverse_blocks_per_sm(OP)) adj_reverse_kernel(const AdjArgs a, const float* pc_prev,
+__global__ void __launch_bounds__(kAdjBlock, kAdjReverseBlocksPerSm) adj_reverse_kernel(const AdjArgs a, const float* pc_prev,
                                                                 const float* lam_next, float* lam_out,
                                                                 const float* avg, int objective, double* g_gamma,
                                                                 double* part, double* avg_part) {
-    constexpr int D = OP == LBMX_CM_OPT ? 16 : 13;  // ps[9], gamma, omega, Fx, Fy [, averages]
     const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     float sums[3] = {0.f, 0.f, 0.f}, asums[3] = {0.f, 0.f, 0.f};
     if (node < a.g.n) {
@@ -652,12 +699,12 @@ __global__ void __launch_bounds__(kAdjBlock, adj_reverse_blocks_per_sm(OP)) adj_
             }
             mu[q] = m;
         }
-        // The collision conserves mass, so a column's tangents sum to an
+        // The collision conserves mass, so a Jacobian column sums to an
         // integer -- 0 for the parameters, 1 (or more where bounce-back copies
         // a population) for a population -- while mu is nearly constant over
-        // q.  Dotting mu - mean(mu) and adding mean(mu) times that integer
-        // keeps FP32 from cancelling mean(mu) against the rounding of the
-        // tangents.
+        // q.  Propagating mu - mean(mu) and adding mean(mu) times that
+        // integer keeps FP32 from cancelling mean(mu) against the rounding
+        // of the Jacobian.
         float c = 0.0f;
 #pragma unroll
         for (int q = 0; q < 9; q++) c += mu[q];
@@ -673,66 +720,12 @@ __global__ void __launch_bounds__(kAdjBlock, adj_reverse_blocks_per_sm(OP)) adj_
             w[2] = a.weights[2 * n + node];
         }
         const float gm = a.gamma ? a.gamma[node] : 0.0f;
-        float s[D];
-        if (OP != LBMX_CM_OPT) {
-            adj_node_vjp<OP>(a, x, y, fl, ps, gm, mu, c, w, s, &s[9], &s[10], &s[11], &s[12]);
-        } else {
-        using R = Dual<kTan>;
-#pragma unroll 1
-        for (int p0 = 0; p0 < D; p0 += kTan) {
-            R f[9], S[9], av[3], mom[3];
-            auto seed = [&](float v, int dir) {
-                R r = dconst<kTan>(v);
+        const float av[3] = {avg ? avg[0] : 1.0f, avg ? avg[1] : 1.0f, avg ? avg[2] : 1.0f};
+        float lam[9], d_gamma;
+        adj_node_vjp<OP>(a, x, y, fl, ps, gm, mu, c, w, av, lam, &d_gamma, &sums[0], &sums[1], &sums[2], asums);
 #pragma unroll
-                for (int k = 0; k < kTan; k++) r.d[k] = (p0 + k == dir) ? 1.0f : 0.0f;
-                return r;
-            };
-#pragma unroll
-            for (int q = 0; q < 9; q++) f[q] = seed(ps[q], q);
-            const R g = seed(gm, 9);
-            const R om = seed(a.omega, 10);
-#pragma unroll
-            for (int k = 0; k < 9; k++) S[k] = seed(a.S[k], ((a.omega_mask >> k) & 1u) ? 10 : -1);
-            const R Fx = seed(a.fx, 11), Fy = seed(a.fy, 12);
-#pragma unroll
-            for (int j = 0; j < 3; j++) av[j] = seed(avg ? avg[j] : 1.0f, 13 + j);
-            adj_bc<R>(a.g, f, x, y, fl);
-            adj_node<R, OP>(a, f, g, Fx, Fy, om, S, av, mom);
-            const R jx = mom[0] * mom[1], jy = mom[0] * mom[2];
-#pragma unroll
-            for (int k = 0; k < kTan; k++) {
-                if (p0 + k >= D) break;
-                float t;
-                if (a.drag) {
-                    // J's node term gamma (w . moments): its gamma column
-                    // gains the explicit term w . moments
-                    const R ob = g * (w[0] * mom[0] + w[1] * jx + w[2] * jy);
-                    t = ob.d[k];
-                } else {
-                    t = w[0] * mom[0].d[k] + w[1] * jx.d[k] + w[2] * jy.d[k];
-                }
-                float tsum = 0.0f;
-#pragma unroll
-                for (int q = 0; q < 9; q++) {
-                    t = fmaf(mu[q], f[q].d[k], t);
-                    tsum += f[q].d[k];
-                }
-                if (p0 + k < 9) t = fmaf(c, rintf(tsum), t);
-                s[p0 + k] = t;
-            }
-        }
-        }
-#pragma unroll
-        for (int q = 0; q < 9; q++) lam_out[q * n + node] = s[q];
-        g_gamma[node] += s[9];
-        sums[0] = s[10];
-        sums[1] = s[11];
-        sums[2] = s[12];
-        if (OP == LBMX_CM_OPT) {
-            asums[0] = s[13 % D];
-            asums[1] = s[14 % D];
-            asums[2] = s[15 % D];
-        }
+        for (int q = 0; q < 9; q++) lam_out[q * n + node] = lam[q];
+        g_gamma[node] += d_gamma;
     }
     adj_block_sum<3, float>(sums, part, true);
     if (OP == LBMX_CM_OPT) {
