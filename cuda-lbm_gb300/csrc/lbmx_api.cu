@@ -123,55 +123,75 @@ StepArgs lbmx::base_args(const lbmx_handle* h) {
 static lbmx_status rebuild_special(lbmx_handle* h) {
     const Geometry& g = h->g;
     const int units_per_row = g.pitch / 2;
-    std::vector<char> interior_special((size_t)g.ny * units_per_row, 0);
+    const uint8_t* F = h->flags_host.empty() ? nullptr : h->flags_host.data();  // pitched, zero past nx
     bool any_interior = false;
-    auto mark = [&](long long off) {
-        const int y = (int)(off / g.pitch), x0 = (int)(off % g.pitch) & ~1;
-        interior_special[(size_t)y * units_per_row + x0 / 2] = 1;
-    };
-    if (!h->flags_host.empty())
-        for (int y = 0; y < g.ny; y++)
-            for (int x = 0; x < g.nx; x++)
-                if (h->flags_host[(size_t)y * g.pitch + x]) mark((long long)y * g.pitch + x);
-    // an own-node step (parity 0) runs a node through the tiles unless it has
-    // a boundary functor or (fluid on a non-periodic edge) reads the edge store
-    auto plain0 = [&](int x, int y) {
-        const size_t off = (size_t)y * g.pitch + x;
-        const uint8_t f = h->flags_host.empty() ? (uint8_t)LBMX_FLUID : h->flags_host[off];
-        if (f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB) return true;
-        const bool edge = (!g.periodic_x && (x == 0 || x == g.nx - 1)) || (!g.periodic_y && (y == 0 || y == g.ny - 1));
-        return f == LBMX_FLUID && !edge;
-    };
     std::vector<int> units, units0;
     std::vector<uint32_t> bits(((size_t)g.ny * units_per_row + 31) / 32, 0u), bits0(bits.size(), 0u);
-    // ghost rows (a y-slab's copies of its neighbours' boundary rows) are in
-    // no unit list; parity 0 marks them so the tiles skip them too, parity 1
-    // tiles skip them as perimeter rows
-    const auto ghost = [&](int y) {
-        return ((h->ghost_mask & 1u) && y == 0) || ((h->ghost_mask & 2u) && y == g.ny - 1);
+    const auto set_bit = [](std::vector<uint32_t>& b, size_t u) { b[u >> 5] |= 1u << (u & 31); };
+    // an own-node step (parity 0) runs a node through the tiles unless it has
+    // a boundary functor or (fluid on a non-periodic edge) reads the edge store
+    const auto plain0 = [](uint8_t f, bool edge) {
+        return f == LBMX_HALFWAY_BB || f == LBMX_MOVING_WALL_BB || (f == LBMX_FLUID && !edge);
     };
-    for (int y = 0; y < g.ny; y++)
-        for (int x0 = 0; x0 < g.nx; x0 += 2) {
-            const bool perim = y == 0 || y == g.ny - 1 || x0 == 0 || x0 + 1 >= g.nx - 1;
-            const size_t u = (size_t)y * units_per_row + x0 / 2;
-            if (ghost(y)) {
-                bits0[u >> 5] |= 1u << (u & 31);
-                continue;
-            }
-            // a y-slab of a y-periodic lattice: the lattice's first and last
-            // rows take the general path of a neighbour-access step, as there
-            const long long wy = h->whole_ny > 0 ? ((h->row_origin + y) % h->whole_ny + h->whole_ny) % h->whole_ny : -1;
-            const bool wrap_row = h->whole_ny > 0 && (wy == 0 || wy == h->whole_ny - 1);
-            if (perim || interior_special[u] || wrap_row) units.push_back(y * g.pitch + x0);
-            if (!perim && (interior_special[u] || wrap_row)) {
-                bits[u >> 5] |= 1u << (u & 31);
+    for (int y = 0; y < g.ny; y++) {
+        const uint8_t* row = F ? F + (size_t)y * g.pitch : nullptr;
+        const size_t u_row = (size_t)y * units_per_row;
+        // ghost rows (a y-slab's copies of its neighbours' boundary rows) are
+        // in no unit list; parity 0 marks them so the tiles skip them too,
+        // parity 1 tiles skip them as perimeter rows
+        if (((h->ghost_mask & 1u) && y == 0) || ((h->ghost_mask & 2u) && y == g.ny - 1)) {
+            for (int x0 = 0; x0 < g.nx; x0 += 2) set_bit(bits0, u_row + x0 / 2);
+            continue;
+        }
+        const bool yedge = y == 0 || y == g.ny - 1;
+        const bool open_y = !g.periodic_y && yedge;
+        // a y-slab of a y-periodic lattice: the lattice's first and last
+        // rows take the general path of a neighbour-access step, as there
+        const long long wy = h->whole_ny > 0 ? ((h->row_origin + y) % h->whole_ny + h->whole_ny) % h->whole_ny : -1;
+        const bool wrap_row = h->whole_ny > 0 && (wy == 0 || wy == h->whole_ny - 1);
+        const auto unit = [&](int x0) {
+            const bool pair = x0 + 1 < g.nx;
+            const uint8_t f0 = row ? row[x0] : (uint8_t)LBMX_FLUID;
+            const uint8_t f1 = row && pair ? row[x0 + 1] : (uint8_t)LBMX_FLUID;
+            const bool perim = yedge || x0 == 0 || x0 + 1 >= g.nx - 1;
+            const bool flagged = (f0 | f1) != 0;
+            const size_t u = u_row + x0 / 2;
+            if (perim || flagged || wrap_row) units.push_back(y * g.pitch + x0);
+            if (!perim && (flagged || wrap_row)) {
+                set_bit(bits, u);
                 any_interior = true;
             }
-            if (x0 + 1 >= g.nx || !plain0(x0, y) || !plain0(x0 + 1, y)) {
+            const bool e0 = open_y || (!g.periodic_x && (x0 == 0 || x0 == g.nx - 1));
+            const bool e1 = open_y || (!g.periodic_x && x0 + 1 == g.nx - 1);
+            if (!pair || !plain0(f0, e0) || !plain0(f1, e1)) {
                 units0.push_back(y * g.pitch + x0);
-                bits0[u >> 5] |= 1u << (u & 31);
+                set_bit(bits0, u);
             }
+        };
+        // the units from last_start on are on the perimeter (x0 + 1 >= nx - 1)
+        const int last_start = std::max(0, (g.nx - 1) & ~1);
+        if (yedge || wrap_row) {
+            for (int x0 = 0; x0 < g.nx; x0 += 2) unit(x0);
+            continue;
         }
+        // elsewhere in the row only a flagged unit can be in a list: skip
+        // fluid nodes eight at a time
+        unit(0);
+        for (int x0 = 2; x0 < last_start;) {
+            if (!row) break;
+            if ((x0 & 7) == 0 && x0 + 8 <= last_start) {
+                uint64_t w;
+                memcpy(&w, row + x0, 8);
+                if (w == 0) {
+                    x0 += 8;
+                    continue;
+                }
+            }
+            if (row[x0] | row[x0 + 1]) unit(x0);
+            x0 += 2;
+        }
+        for (int x0 = std::max(2, last_start); x0 < g.nx; x0 += 2) unit(x0);
+    }
     // Work that touches the IBM patch goes last: with the IBM kernel still
     // running, the step kernel takes every other item first.  A node's update
     // reads and writes only its own AA slots and reads its own force entry,
@@ -201,24 +221,31 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
         return (int)(it - list.begin());
     };
     const int indep = by_patch(units), indep0 = by_patch(units0);
-    cudaFree(h->special_units);
-    cudaFree(h->special_bits);
-    cudaFree(h->special_units0);
-    cudaFree(h->special_bits0);
-    h->special_units = h->special_units0 = nullptr;
+    // device copies, in buffers that only grow (a cudaFree / cudaMalloc pair
+    // per list cost about as much as building the lists); null unit bits:
+    // none marked
+    LBMX_CUDA(h, cudaStreamSynchronize(h->stream));
+    const auto upload = [&](const void* src, size_t bytes, void** buf, size_t* cap) -> cudaError_t {
+        if (!*buf || *cap < bytes) {
+            cudaFree(*buf);
+            *buf = nullptr;
+            *cap = 0;
+            const cudaError_t e = cudaMalloc(buf, std::max<size_t>(bytes, 4));
+            if (e != cudaSuccess) return e;
+            *cap = std::max<size_t>(bytes, 4);
+        }
+        return bytes ? cudaMemcpy(*buf, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+    };
+    LBMX_CUDA(h, upload(units.data(), units.size() * sizeof(int), (void**)&h->special_units, &h->cap_units));
+    LBMX_CUDA(h, upload(units0.data(), units0.size() * sizeof(int), (void**)&h->special_units0, &h->cap_units0));
     h->special_bits = h->special_bits0 = nullptr;
-    LBMX_CUDA(h, cudaMalloc((void**)&h->special_units, std::max<size_t>(1, units.size()) * sizeof(int)));
-    LBMX_CUDA(h, cudaMemcpy(h->special_units, units.data(), units.size() * sizeof(int), cudaMemcpyHostToDevice));
     if (any_interior) {
-        LBMX_CUDA(h, cudaMalloc((void**)&h->special_bits, bits.size() * sizeof(uint32_t)));
-        LBMX_CUDA(h, cudaMemcpy(h->special_bits, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        LBMX_CUDA(h, upload(bits.data(), bits.size() * sizeof(uint32_t), (void**)&h->bits_buf, &h->cap_bits));
+        h->special_bits = h->bits_buf;
     }
-    LBMX_CUDA(h, cudaMalloc((void**)&h->special_units0, std::max<size_t>(1, units0.size()) * sizeof(int)));
-    if (!units0.empty())
-        LBMX_CUDA(h, cudaMemcpy(h->special_units0, units0.data(), units0.size() * sizeof(int), cudaMemcpyHostToDevice));
     if (!units0.empty() || h->ghost_mask) {
-        LBMX_CUDA(h, cudaMalloc((void**)&h->special_bits0, bits0.size() * sizeof(uint32_t)));
-        LBMX_CUDA(h, cudaMemcpy(h->special_bits0, bits0.data(), bits0.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        LBMX_CUDA(h, upload(bits0.data(), bits0.size() * sizeof(uint32_t), (void**)&h->bits0_buf, &h->cap_bits0));
+        h->special_bits0 = h->bits0_buf;
     }
     h->nspecial = (int)units.size();
     h->special_chunks = (2 * h->nspecial + kSpecialChunk - 1) / kSpecialChunk;
@@ -356,8 +383,8 @@ void lbmx_destroy(lbmx_handle* h) {
     cudaFree(h->f_alloc); cudaFree(h->flags); cudaFree(h->edge); cudaFree(h->aux);
     cudaFree(h->force); cudaFree(h->gamma); cudaFree(h->rho_out); cudaFree(h->u_out); cudaFree(h->staging);
     cudaFree(h->pop_out); cudaFree(h->partials); cudaFree(h->counter); cudaFree(h->sums); cudaFree(h->raw_sums);
-    cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->special_bits);
-    cudaFree(h->special_units0); cudaFree(h->special_bits0); cudaFree(h->tile_order);
+    cudaFree(h->avg); cudaFree(h->error_word); cudaFree(h->special_units); cudaFree(h->bits_buf);
+    cudaFree(h->special_units0); cudaFree(h->bits0_buf); cudaFree(h->tile_order);
     cudaFree(h->tile_counter);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     cudaSetDevice(cur);
@@ -464,11 +491,29 @@ lbmx_status lbmx_set_flags(lbmx_handle* h, const uint8_t* flags) {
     const Geometry& g = h->g;
     const long long n = (long long)g.nx * g.ny;
     std::vector<uint8_t> hf(n);
-    LBMX_CUDA(h, cudaMemcpy(hf.data(), flags, n, cudaMemcpyDefault));
+    // host memory (pinned or not) is read directly, device memory copied
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, flags) == cudaSuccess &&
+        (pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeUnregistered)) {
+        memcpy(hf.data(), flags, (size_t)n);
+    } else {
+        cudaGetLastError();
+        LBMX_CUDA(h, cudaMemcpy(hf.data(), flags, n, cudaMemcpyDefault));
+    }
     bool any = false, aux = false;
     for (int y = 0; y < g.ny; y++)
         for (int x = 0; x < g.nx; x++) {
-            const uint8_t fl = hf[(long long)y * g.nx + x];
+            const uint8_t* r = &hf[(long long)y * g.nx];
+            // eight fluid nodes at a time
+            if ((x & 7) == 0 && x + 8 <= g.nx) {
+                uint64_t w;
+                memcpy(&w, r + x, 8);
+                if (w == 0) {
+                    x += 7;
+                    continue;
+                }
+            }
+            const uint8_t fl = r[x];
             if (fl == 0) continue;
             any = true;
             const bool edge = x == 0 || y == 0 || x == g.nx - 1 || y == g.ny - 1;

@@ -59,6 +59,9 @@ struct lbmx_handle {
     uint32_t* special_bits = nullptr;
     int* special_units0 = nullptr;
     uint32_t* special_bits0 = nullptr;
+    uint32_t* bits_buf = nullptr;     // the storage behind special_bits / special_bits0 (which may be null)
+    uint32_t* bits0_buf = nullptr;
+    size_t cap_units = 0, cap_units0 = 0, cap_bits = 0, cap_bits0 = 0;  // bytes of the four buffers
     int nspecial0 = 0, special_chunks0 = 0;
     int dep_chunk = 0, dep_chunk0 = 0;  // first chunk of each list with units next to the IBM patch
     int* tile_order = nullptr;          // tiles away from the IBM patch, then the others (null without markers)

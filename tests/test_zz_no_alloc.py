@@ -98,3 +98,34 @@ def test_noalloc_rejects_bad_sizes():
     assert L.lib.lbmx_moment_sums_noalloc(rho.data_ptr(), u.data_ptr(), 0, ctypes.addressof(out), None) == 1
     too_big = 2 ** 31
     assert L.lib.lbmx_moment_sums_noalloc(rho.data_ptr(), u.data_ptr(), too_big, ctypes.addressof(out), None) == 8
+
+
+def test_noalloc_call_captured_in_a_cuda_graph():
+    """With its sums going to device memory the call never synchronises, so
+    it can be captured into a CUDA graph (after a first call outside any
+    capture, which resolves the library's scratch array); every replay
+    writes the sums of the fields' values at that time."""
+    import torch
+
+    c = C.taylor_green(64, 32)
+    L = C.make_lattice(c)
+    n = 256 * 128
+    rng = np.random.default_rng(3)
+    rho = torch.from_numpy(rng.uniform(0.9, 1.1, n).astype(np.float32)).cuda()
+    u = torch.from_numpy(rng.normal(0.0, 0.05, 2 * n).astype(np.float32)).cuda()
+    first = _host_call(L, rho, u)
+    out = torch.full((3,), -1.0, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        assert _noalloc(L, rho, u, out.data_ptr(), s.cuda_stream) == 0
+    g.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), first)
+    rho.mul_(1.5)
+    u.mul_(-2.0)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), _host_call(L, rho, u))
