@@ -88,6 +88,30 @@ __device__ __forceinline__ void warp_sums(double* partials, const Acc v[kNumSums
     }
 }
 
+// kModeSums: mass and momentum of the whole CTA (warp shuffles, the warps'
+// totals added in shared memory), one atomic per sum into the CTA's slot --
+// at the end of a step every CTA reduces at once, and one atomic per warp
+// queued on the 32 slots' addresses.  Every thread of the CTA calls it.
+__device__ __forceinline__ void cta_sums(double* partials, const Acc v[kNumSums]) {
+    __shared__ Acc sh[kStepThreads / 32][3];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        Acc t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[warp][k] = t;
+    }
+    __syncthreads();
+    if (tid < 3) {
+        Acc t = 0;
+#pragma unroll
+        for (int w = 0; w < kStepThreads / 32; w++) t += sh[w][tid];
+        unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials) + (blockIdx.x % kSumSlots) * kNumSums;
+        if (t != 0) atomicAdd(acc + tid, (unsigned long long)t);
+    }
+}
+
 // The sums in `mask` of an accumulator set (integer sums over the slots: the
 // same bits in any order), zeroing them for their next use; the others are 0.
 __device__ __forceinline__ void collect_sums(double* partials, unsigned mask, double s[kNumSums],
@@ -651,9 +675,9 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
     }
     // an early-started grid finishes only after the grid it overlapped
     if (a.early) asm volatile("griddepcontrol.wait;" ::: "memory");
-    // kModeSums: each warp adds its totals and is done (the next launch
+    // kModeSums: each CTA adds its totals and is done (the next launch
     // publishes them); kModeFull: the last CTA publishes
-    if (MODE == kModeSums) warp_sums(a.partials, v, sums_mask(false, false));
+    if (MODE == kModeSums) cta_sums(a.partials, v);
     else if (MODE == kModeFull && a.partials) block_sums(a, v, (long long)a.g.nx * a.g.ny);
 }
 
