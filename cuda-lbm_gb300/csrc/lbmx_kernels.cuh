@@ -112,22 +112,30 @@ __device__ __forceinline__ void cta_sums(double* partials, const Acc v[kNumSums]
     }
 }
 
-// The sums in `mask` of an accumulator set (integer sums over the slots: the
-// same bits in any order), zeroing them for their next use; the others are 0.
-__device__ __forceinline__ void collect_sums(double* partials, unsigned mask, double s[kNumSums],
-                                             long long* raw = nullptr) {
-    unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials);
+// The sums in `mask` of an accumulator set, by one warp: lane j takes slot j
+// (integer totals, the same bits in any order), in one round of loads; the
+// slots are zeroed for their next use.  Every lane gets s (the other sums 0);
+// lane 0 writes raw when given.
+static_assert(kSumSlots == 32, "collect_sums: one slot per lane");
+__device__ __forceinline__ void collect_sums(double* partials, unsigned mask, double s[kNumSums], long long* raw,
+                                             int lane) {
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials) + lane * kNumSums;
+    unsigned long long t[kNumSums];
+#pragma unroll
     for (int k = 0; k < kNumSums; k++) {
-        s[k] = 0.0;
-        if (raw) raw[k] = 0;
-        if (!((mask >> k) & 1u)) continue;
-        unsigned long long t = 0;
-        for (int j = 0; j < kSumSlots; j++) {
-            t += __ldcg(acc + j * kNumSums + k);
-            acc[j * kNumSums + k] = 0ull;
+        t[k] = 0ull;
+        if ((mask >> k) & 1u) {
+            t[k] = __ldcg(acc + k);
+            acc[k] = 0ull;
         }
-        s[k] = (double)(long long)t * (1.0 / (double)kFixScale);
-        if (raw) raw[k] = (long long)t;
+    }
+#pragma unroll
+    for (int k = 0; k < kNumSums; k++) {
+        if ((mask >> k) & 1u)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+        s[k] = (double)(long long)t[k] * (1.0 / (double)kFixScale);
+        if (raw && lane == 0) raw[k] = (long long)t[k];
     }
 }
 
@@ -142,28 +150,11 @@ __device__ __forceinline__ void write_sums(const double s[kNumSums], double* sum
     }
 }
 
-// Publish a kModeSums step's sums: mass and momentum only.  One warp, lane
-// j taking slot j of each sum (the same integer totals as a serial loop, in
-// one round of loads instead of three).
-static_assert(kSumSlots == 32, "publish_sums: one slot per lane");
+// Publish a kModeSums step's sums (mass and momentum only), by one warp.
 __device__ __forceinline__ void publish_sums(double* partials, double* sums, double* series, int lane) {
-    unsigned long long* acc = reinterpret_cast<unsigned long long*>(partials) + lane * kNumSums;
-    unsigned long long t[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        t[k] = __ldcg(acc + k);
-        acc[k] = 0ull;
-    }
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_down_sync(0xffffffffu, t[k], o);
-    if (lane == 0) {
-        double sv[kNumSums] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int k = 0; k < 3; k++) sv[k] = (double)(long long)t[k] * (1.0 / (double)kFixScale);
-        write_sums(sv, sums, series, false);
-    }
+    double sv[kNumSums];
+    collect_sums(partials, sums_mask(false, false), sv, nullptr, lane);
+    if (lane == 0) write_sums(sv, sums, series, false);
 }
 
 // Grid reduction of the accumulators; the last CTA to finish publishes the
@@ -180,10 +171,11 @@ __device__ __forceinline__ void block_sums(const StepArgs& a, const Acc v[kNumSu
         is_last = (done == gridDim.x - 1);
     }
     __syncthreads();
-    if (!is_last || tid != 0) return;
+    if (!is_last || tid >= 32) return;
     __threadfence();
     double s[kNumSums];
-    collect_sums(a.partials, mask, s, a.raw_sums);
+    collect_sums(a.partials, mask, s, a.raw_sums, tid);
+    if (tid != 0) return;
     write_sums(s, a.sums, a.series, a.ke != 0);
     if (a.avg_out) {
         a.avg_out[0] = (float)(s[0] / (double)n_nodes);
