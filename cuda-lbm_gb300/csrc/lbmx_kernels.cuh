@@ -594,9 +594,17 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepAr
                 break;
             }
             if (left == 0) {
-                int base = 0;
-                if (lane == 0) base = (int)atomicAdd(a.tile_counter, (unsigned long long)a.tile_chunk);
-                next = __shfl_sync(0xffffffffu, base, 0);
+                // the first claim of every CTA is its own block of items (no
+                // atomic: all CTAs claim at once at the start); the counter
+                // hands out the items after those
+                int base = (int)blockIdx.x * a.tile_chunk;
+                if (k > 0) {
+                    if (lane == 0)
+                        base = (int)gridDim.x * a.tile_chunk +
+                               (int)atomicAdd(a.tile_counter, (unsigned long long)a.tile_chunk);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                }
+                next = base;
                 left = a.tile_chunk;
             }
             const int item = next++;
