@@ -280,17 +280,24 @@ static lbmx_status rebuild_special(lbmx_handle* h) {
         LBMX_CUDA(h, cudaMemcpy(h->tile_order, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
     // Persistent CTAs walk the work list, kCtasPerSm per SM, except in the
-    // steps of a small lattice (fewer than 16 items per CTA) that have
-    // general-path chunks: there two per SM.  A chunk is one node per
-    // thread, a long chain of dependent loads and arithmetic that a third
-    // CTA on the SM stretches past the end of the tiles (on a 1024^2 cavity
-    // 9 -> 14 us), while without chunks the third CTA hides more of the
-    // tiles' latency (13.3 -> 11.5 us).  Claims take about 1/16 of a CTA's
-    // share: few atomics on large lattices, one item at a time on small ones.
+    // steps with general-path chunks of a lattice so small that three CTAs
+    // per SM would get fewer than four items each: there two per SM.  A
+    // chunk is one node per thread, a long chain of dependent loads and
+    // arithmetic that a third CTA on the SM stretches (9 -> 14 us on a 1024^2
+    // cavity); with only two or three tiles to follow it, its CTA then ends
+    // last (the 1024^2 FP16 step with 128 x 8 tiles: 16.4 us flushed with
+    // two CTAs per SM in its neighbour-access steps, 18.4 with three; the
+    // FP32 step with 128 x 4 tiles: 16.4 with three, 18.4 with two).  With
+    // IBM markers, two per SM below 16 items per CTA: the step's grid then
+    // fits beside the IBM kernel's CTA it overlaps (the 2048 x 512 cylinder
+    // 16.8 us a step with two, 17.3 with three).  Claims take about 1/16 of
+    // a CTA's share: few atomics on large lattices, one item at a time on
+    // small ones.
     const long long tiles = (long long)h->tiles_x * h->tiles_y;
+    const long long few = (h->patch_host.empty() ? 4LL : 16LL) * kCtasPerSm * h->num_sms;
     const auto split = [&](int chunks, int* num_ctas, int* tile_chunk) {
         const long long items = tiles + chunks;
-        const int per_sm = (items >= 16LL * kCtasPerSm * h->num_sms || chunks == 0) ? kCtasPerSm : 2;
+        const int per_sm = (items >= few || chunks == 0) ? kCtasPerSm : 2;
         *num_ctas = (int)std::max<long long>(1, std::min<long long>(items, (long long)per_sm * h->num_sms));
         *tile_chunk = (int)std::max<long long>(1, items / (16LL * *num_ctas));
     };

@@ -3,9 +3,9 @@
 // lbmx_batch_{f32,f16,bf16}.cu.
 //
 // The reference steps one lattice per process (src/main.cu:96-114).  Here a
-// work list holds, for every lattice of a batch, its chunks of special units
-// (perimeter and flagged nodes, general path) followed by its interior tiles
-// (TMA-staged, packed FP32x2 collision): the same two paths as the
+// work list holds, for every lattice of a batch, its interior tiles
+// (TMA-staged, packed FP32x2 collision) followed by its chunks of special
+// units (perimeter and flagged nodes, general path): the same two paths as the
 // single-lattice step kernel, with the lattice read from the work item.  All
 // CTAs are persistent and warp-specialised; the producer warp claims items
 // from one counter, fills the stage ring with the item's tile (nothing for a
@@ -50,9 +50,15 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && TW * TH > kStageW
                 break;
             }
             if (left == 0) {
-                int base = 0;
-                if (lane == 0) base = (int)atomicAdd(b.counter, (unsigned long long)b.chunk);
-                next = __shfl_sync(0xffffffffu, base, 0);
+                // the first claim of every CTA is its own block of items (no
+                // atomic at the start); the counter hands out the rest
+                int base = (int)blockIdx.x * b.chunk;
+                if (k > 0) {
+                    if (lane == 0)
+                        base = (int)gridDim.x * b.chunk + (int)atomicAdd(b.counter, (unsigned long long)b.chunk);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                }
+                next = base;
                 left = b.chunk;
             }
             const int item = next++;
