@@ -497,7 +497,10 @@ lbmx_status lbmx_set_flags(lbmx_handle* h, const uint8_t* flags) {
     cudaSetDevice(h->p.device);
     const Geometry& g = h->g;
     const long long n = (long long)g.nx * g.ny;
-    std::vector<uint8_t> hf(n);
+    // a staging buffer kept with the handle: a fresh megabyte each call came
+    // from new pages, faulted in on first touch
+    std::vector<uint8_t>& hf = h->flags_in;
+    hf.resize((size_t)n);
     // host memory (pinned or not) is read directly, device memory copied
     cudaPointerAttributes pa;
     if (cudaPointerGetAttributes(&pa, flags) == cudaSuccess &&

@@ -53,6 +53,7 @@ struct lbmx_handle {
     std::vector<int> patch_host;   // IBM patch node offsets
     // work split of the step kernel
     std::vector<uint8_t> flags_host;  // pitched copy of the flags (empty: all fluid)
+    std::vector<uint8_t> flags_in;    // lbmx_set_flags' dense copy of the caller's flags
     // general-path units of a neighbour-access step (parity 1) and of an
     // own-node step (parity 0)
     int* special_units = nullptr;
