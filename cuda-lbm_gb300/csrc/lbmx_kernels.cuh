@@ -523,13 +523,14 @@ template <typename T, int OP, int P, int MODE>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) step_kernel(const StepArgs a, const __grid_constant__ CUtensorMap tmap) {
     constexpr int TW = step_tile_w((int)sizeof(T)), TH = step_tile_h((int)sizeof(T));
     // Persistent CTAs, warp-specialised: warp 8 produces (claims the next
-    // work item from a global counter; for an interior tile it bulk-copies
-    // the tile into the ring), warps 0-7 consume.  Items 0..dep_chunk-1
-    // are chunks of special nodes (general path, one node per consumer
-    // thread, nothing staged) so the boundary work spreads over every SM;
-    // the interior tiles follow, then the chunks next to an IBM patch.  full[s] completes when a stage's bytes have
-    // landed (or at once for a special chunk); empty[s] when all eight
-    // consumer warps are done with it.
+    // work items, its CTA's own block first and then from a global counter;
+    // for an interior tile it bulk-copies the tile into the ring), warps 0-7
+    // consume.  Items 0..dep_chunk-1 are chunks of special nodes (general
+    // path, one node per consumer thread, nothing staged) so the boundary
+    // work spreads over every SM; the interior tiles away from an IBM patch
+    // follow, then the chunks and the tiles next to one.  full[s] completes
+    // when a stage's bytes have landed (or at once for a special chunk);
+    // empty[s] when all eight consumer warps are done with it.
     using St = Staging<T, TW, TH>;
     Acc v[kNumSums] = {0, 0, 0, 0, 0, 0};
     const int tid = threadIdx.x;
